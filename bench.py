@@ -1,0 +1,330 @@
+"""Benchmark of the transport-map hot path on one GB300 (or N replicas).
+
+Workload (one "step" = one transport map): the single-day-pair configuration,
+20,000 x 25,000 synthetic cells, 1,000 genes, 20 clusters, local PCA 30,
+default wot parameters (epsilon 0.05, lambda1 1, lambda2 50, epsilon0 1,
+tau 1e4, tolerance 1e-8, duality-gap solver) and growth_iters = 3. A step runs
+the cost kernel, the exact FP32 median, three full duality-gap solves and the
+dense FP64 coupling, on device-resident coordinates (value), and the whole
+OTModel.compute_transport_map call on host data (e2e).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0). Under torchrun each rank solves its own pair
+(seed + rank): weak scaling with no data-path collective.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "OT maps/sec @≤1e-4 coupling err, batched vs plain, 1×GB300; Sinkhorn iter/s"
+CFG = dict(growth_iters=3, epsilon=0.05, lambda1=1, lambda2=50, epsilon0=1, tau=10000, scaling_iter=3000,
+           inner_iter_max=50, tolerance=1e-8, max_iter=1e7, batch_size=5, extra_iter=1000)
+I_FULL, J_FULL, GENES, CLUSTERS, PCA_D = 20000, 25000, 1000, 20, 30
+SAMPLE = (2000, 2500)          # bounded CPU sample of the same cells
+REF_SAMPLE = (1000, 1250)      # per-step sample of the reference arm
+WORKLOAD = ('single day pair 20000x25000 cells, 1000 genes, 20 clusters, local_pca=30, growth_iters=3, '
+            'duality-gap solver, eps=0.05 lambda1=1 lambda2=50 eps0=1 tau=1e4 tol=1e-8')
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=3)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)), int(os.environ.get('LOCAL_RANK', 0))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            p = json.load(f)
+        return float(p['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+         'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+         'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.Q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ''
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in getattr(self, 'lines', []):
+            f = [x.strip() for x in ln.split(',')]
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+                for k, n in enumerate(names):
+                    if f[5 + k].lower().startswith('active'):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': mx, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def make_pair(seed, I=I_FULL, J=J_FULL):
+    from wot_gb300 import synthetic
+    X, day, growth = synthetic.time_course([I, J], n_genes=GENES, n_clusters=CLUSTERS, seed=seed)
+    return X, day, growth
+
+
+def coords_on_device(X, day):
+    from wot_gb300.ot.util import compute_pca
+    x0, x1, s, _ = compute_pca(X[day == 0], X[day == 1], PCA_D)
+    return (x0 * s).float().contiguous(), (x1 * s).float().contiguous()
+
+
+def cpu_sample(a, b, G, I_s, J_s, rng):
+    """Oracle (FP64 NumPy restatement) on a random cell subsample; returns
+    (seconds, iterations, coupling, (a_s, b_s, G_s))."""
+    from oracle import ot_model as oom, optimal_transport as oot
+    ri = np.sort(rng.choice(a.shape[0], I_s, replace=False))
+    rj = np.sort(rng.choice(b.shape[0], J_s, replace=False))
+    a_s, b_s, G_s = a[ri].astype(np.float64), b[rj].astype(np.float64), G[ri]
+    t0 = time.perf_counter()
+    C = oom.compute_default_cost_matrix(a_s, b_s)
+    iters = [0]
+
+    def counting(**kw):
+        st = {}
+        out = oot.optimal_transport_duality_gap(stats=st, **kw)
+        iters[0] += st['iterations']
+        return out
+
+    T, _ = oot.compute_transport_matrix(solver=counting, C=C, G=G_s.copy(), **CFG)
+    return time.perf_counter() - t0, iters[0], T, (a_s, b_s, G_s)
+
+
+def blas_threads():
+    for k in ('OPENBLAS_NUM_THREADS', 'OMP_NUM_THREADS', 'MKL_NUM_THREADS'):
+        if os.environ.get(k):
+            return int(os.environ[k])
+    return os.cpu_count() or 1
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU algorithm (the oracle port; the
+    reference itself is not available on the GPU host) on bounded samples of
+    the same workload, extrapolated to the full pair by I*J*iterations."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    X, day, growth = make_pair(1)
+    from oracle import ot_model as oom
+    x0, x1, s, _ = oom.compute_pca(X[day == 0], X[day == 1], PCA_D)
+    a, b, G = x0 * s, x1 * s, growth[day == 0]
+    rng = np.random.default_rng(0)
+    I_s, J_s = REF_SAMPLE
+    times, its = [], []
+    for k in range(args.warmup + args.steps):
+        t, it, _, _ = cpu_sample(a, b, G, I_s, J_s, rng)
+        if k >= args.warmup:
+            times.append(t)
+            its.append(it)
+    t_step = float(np.mean(times))
+    it_s = float(np.mean(its))
+    scale = (I_FULL * J_FULL) / (I_s * J_s)
+    # maps/s at full size assuming the same iteration count as the sample
+    value = 1.0 / (t_step * scale)
+    sample = ('%dx%d random cell subsample of the 20000x25000 pair per step (own median), full FP64 oracle '
+              'duality-gap solve x3 growth iterations (%.0f iterations); maps/s extrapolated by I*J' % (I_s, J_s, it_s))
+    line = {'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': 'maps/s', 'n_gpus': args.gpus,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': t_step * scale * 1e3,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': WORKLOAD, 'I': I_FULL, 'J': J_FULL, 'd': PCA_D},
+            'sinkhorn_iter_per_s': it_s / t_step * (I_s * J_s) / (I_FULL * J_FULL),
+            'cpu_baseline': {'value': value, 'unit': 'maps/s', 'cores': blas_threads(), 'kind': 'port',
+                             'sample': sample},
+            'e2e': {'value': value, 'unit': 'maps/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        run_reference(args)
+        return
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+        pg = dist
+    from wot_gb300 import _build, _native
+    _build.build()
+    lib = _native.load()
+    import wot_gb300 as wot
+    from wot_gb300.ot import device as D
+
+    X, day, growth = make_pair(1 + rank)
+    a, b = coords_on_device(X, day)
+    G = torch.as_tensor(growth[day == 0], device='cuda')
+    tmap = torch.empty((I_FULL, J_FULL), dtype=torch.float64, device='cuda')
+    stream = torch.cuda.current_stream()
+
+    def step():
+        cost = D.default_cost(a, b)
+        return D.solve(cost, G, CFG, _native.SOLVER_DUALITY_GAP, want_tmap=True, tmap_out=tmap)
+
+    for _ in range(args.warmup):
+        res = step()
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    n_launch0 = lib.wotg_launch_count()
+    iters = 0
+    with Clocks(local) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            res = step()
+            iters += res.stats['iterations']
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.wotg_launch_count() - n_launch0
+    t = ev0.elapsed_time(ev1) / 1e3
+    if pg:
+        tt = torch.tensor([t], device='cuda')
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        t = float(tt.item())
+    value = world * args.steps / t
+
+    # dominant kernel: the streaming row half-step over the FP32 cost
+    cost = D.default_cost(a, b)
+    ldc = cost.ldc
+    w = torch.zeros(ldc, dtype=torch.float32, device='cuda')
+    L = torch.empty(I_FULL, dtype=torch.float64, device='cuda')
+    L2 = torch.empty(J_FULL, dtype=torch.float64, device='cuda')
+    wr = torch.zeros(I_FULL, dtype=torch.float32, device='cuda')
+    ws = torch.empty(lib.wotg_lse_matvec_workspace_bytes(I_FULL, J_FULL, ldc), dtype=torch.uint8, device='cuda')
+    import ctypes
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    k2 = ctypes.c_float(float(cost.scale / CFG['epsilon'] * 1.4426950408889634))
+    reps = 20
+    durs = {}
+    for axis, wv, Lv in ((0, w, L), (1, wr, L2)):
+        for _ in range(3):
+            lib.wotg_lse_matvec(cost.C.data_ptr(), I_FULL, J_FULL, ldc, wv.data_ptr(), k2, axis, Lv.data_ptr(),
+                                ws.data_ptr(), ws.numel(), sh)
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps)]
+        for r in range(reps):
+            evs[2 * r].record(stream)
+            st = lib.wotg_lse_matvec(cost.C.data_ptr(), I_FULL, J_FULL, ldc, wv.data_ptr(), k2, axis,
+                                     Lv.data_ptr(), ws.data_ptr(), ws.numel(), sh)
+            evs[2 * r + 1].record(stream)
+            assert st == 0
+        torch.cuda.synchronize()
+        durs[axis] = float(np.mean([evs[2 * r].elapsed_time(evs[2 * r + 1]) for r in range(reps)])) / 1e3
+    alg_bytes = I_FULL * J_FULL * 4 + (J_FULL + I_FULL) * 12
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / durs[0] / 1e9
+    roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
+                'traffic': None, 'kernel': 'row_pass_kernel (wotg_lse_matvec axis 0)', 'peak_kind': peak_kind,
+                'col_pass_GBps': alg_bytes / durs[1] / 1e9,
+                'row_pass_ms': durs[0] * 1e3, 'col_pass_ms': durs[1] * 1e3}
+    del cost
+
+    line = {'metric': METRIC, 'value': value, 'unit': 'maps/s', 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': t / args.steps * 1e3, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': WORKLOAD, 'I': I_FULL, 'J': J_FULL, 'd': PCA_D, 'parallelism': 'replicas' if world > 1 else 'single',
+                       'l2': 'inputs larger than L2 (FP32 cost 2.0 GB per pass)',
+                       'timed': 'cost + median + 3 duality-gap solves + dense FP64 coupling, coordinates resident'},
+            'sinkhorn_iter_per_s': iters / t * world, 'iterations_per_map': iters / args.steps,
+            'roofline': roofline, 'gpu_launches': int(launches), 'clocks': clk.summary()}
+
+    if rank == 0 and not args.no_cpu:
+        rng = np.random.default_rng(0)
+        a_h, b_h, G_h = a.double().cpu().numpy(), b.double().cpu().numpy(), growth[day == 0]
+        t_cpu, it_cpu, T_cpu, (a_s, b_s, G_s) = cpu_sample(a_h, b_h, G_h, SAMPLE[0], SAMPLE[1], rng)
+        scale = (I_FULL * J_FULL) / (SAMPLE[0] * SAMPLE[1])
+        it_gpu = iters / args.steps
+        cpu_value = 1.0 / (t_cpu * scale * (it_gpu / it_cpu))
+        res_s = D.solve(D.default_cost(a_s.astype(np.float32), b_s.astype(np.float32)), G_s, CFG, 0)
+        T_gpu = res_s.tmap.cpu().numpy()
+        line['parity_sample'] = {'shape': list(SAMPLE), 'coupling_max_rel_err':
+                                 float(np.abs(T_gpu - T_cpu).max() / np.abs(T_cpu).max()),
+                                 'iterations_gpu': res_s.stats['iterations'], 'iterations_oracle': it_cpu}
+        line['cpu_baseline'] = {'value': cpu_value, 'unit': 'maps/s', 'cores': blas_threads(), 'kind': 'port',
+                                'sample': '%dx%d random subsample of the pair, full FP64 oracle solve with 3 growth '
+                                          'iterations (%.1f s, %d iterations); extrapolated to 20000x25000 by '
+                                          'I*J*iterations' % (SAMPLE[0], SAMPLE[1], t_cpu, it_cpu)}
+
+    if not args.no_e2e:
+        ids = np.array(['c%d' % i for i in range(len(day))])
+        ds = wot.Dataset(X, wot.Frame({'day': day, 'cell_growth_rate': growth}, index=ids))
+        model = wot.OTModel(ds, growth_iters=3)
+        model.compute_transport_map(0, 1)
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            tm = model.compute_transport_map(0, 1)
+        torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        if pg:
+            tt = torch.tensor([te], device='cuda')
+            pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+            te = float(tt.item())
+        line['e2e'] = {'value': world * args.steps / te, 'unit': 'maps/s',
+                       'h2d_bytes_per_step': int(X.shape[0] * X.shape[1] * 8 + I_FULL * 8),
+                       'd2h_bytes_per_step': int(I_FULL * J_FULL * 8 + 3 * I_FULL * 8),
+                       'api': 'wot_gb300.OTModel(Dataset).compute_transport_map(0, 1) (device PCA + cost + solve)'}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,156 @@
+/*
+ * wotg.h — C ABI of the GB300-native transport-map library (libwotg.so).
+ *
+ * The reference (wot 1.0.8) is pure Python/NumPy; it has no FFI of its own.
+ * Each entry point below replaces one NumPy-level operation or Python function
+ * of the reference's transport-map path, cited as file:line inside the
+ * reference project, and is what a ctypes / cffi binding of that path binds
+ * (see INTEGRATION.md for the binding).
+ *
+ * Conventions
+ *  - All array arguments are DEVICE pointers owned by the caller; the library
+ *    keeps no state between calls and allocates no device memory: every call
+ *    that needs scratch takes a caller-provided workspace whose size comes from
+ *    the matching *_workspace_bytes() query.
+ *  - Dense cost matrices are FP32, row-major, I rows of `ldc` floats with
+ *    ldc >= J and ldc % 4 == 0 (16-byte rows for 128-bit loads); columns
+ *    [J, ldc) are padding and must hold +INFINITY (the cost writers do this).
+ *  - `stream` is a cudaStream_t passed as void* (0 = legacy default stream).
+ *  - Every function returns a wotg_status. WOTG_MAX_ITER is a warning: outputs
+ *    are valid and follow the reference's max_iter behaviour.
+ */
+#ifndef WOTG_H
+#define WOTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum wotg_status {
+  WOTG_OK = 0,
+  WOTG_MAX_ITER = 1,      /* reference: logger.warning + early return, optimal_transport.py:143-145 */
+  WOTG_NONFINITE = 2,     /* reference: RuntimeError on NaN duality gap, optimal_transport.py:162-163 */
+  WOTG_BADARG = 3,        /* reference: ValueError / TypeError on bad inputs */
+  WOTG_CUDA_ERROR = 4,    /* a CUDA runtime call failed; see wotg_last_error() */
+  WOTG_WORKSPACE = 5      /* workspace pointer NULL or smaller than *_workspace_bytes() */
+} wotg_status;
+
+typedef enum wotg_solver {
+  WOTG_SOLVER_DUALITY_GAP = 0, /* optimal_transport_duality_gap, optimal_transport.py:67-164 (default) */
+  WOTG_SOLVER_FIXED_ITERS = 1  /* transport_stablev2, optimal_transport.py:167-236 */
+} wotg_solver;
+
+/* The reference's ot_config keys that reach the solver (ot_model.py:85-87). */
+typedef struct wotg_params {
+  double epsilon;
+  double lambda1;
+  double lambda2;
+  double epsilon0;
+  double tau;
+  double tolerance;
+  double max_iter;
+  int32_t batch_size;
+  int32_t scaling_iter;
+  int32_t inner_iter_max;
+  int32_t extra_iter;
+  int32_t growth_iters;
+  int32_t solver;         /* wotg_solver */
+} wotg_params;
+
+/* Counters of one compute_transport_matrix call (no counterpart in the reference). */
+typedef struct wotg_stats {
+  int64_t iterations;     /* Sinkhorn iterations summed over growth iterations */
+  int64_t absorptions;    /* tau-absorptions (max|a|,|b| > tau) */
+  int64_t checks;         /* stage-exit / duality-gap evaluations */
+  double gap;             /* last relative duality gap (duality_gap solver) */
+  double final_epsilon;   /* epsilon of the last stage */
+  int32_t hit_max_iter;
+  int32_t padding_;
+} wotg_stats;
+
+/* One transport problem: a dense cost and the source growth G.
+ * The reference's cost is cost_scale * C (cost_scale = 1/median for the default
+ * cost, ot_model.py:252; 1 for a user-supplied cost, ot_model.py:307-311). */
+typedef struct wotg_problem {
+  int64_t I;              /* source cells (rows) */
+  int64_t J;              /* target cells (columns) */
+  const float* C;         /* device, I x ldc */
+  int64_t ldc;
+  double cost_scale;
+  const double* G;        /* device, I (growth at the source day) */
+} wotg_problem;
+
+/* Library version string and last CUDA error text (host memory, static). */
+const char* wotg_version(void);
+const char* wotg_last_error(void);
+/* Number of kernels this library has launched in this process (no counterpart
+ * in the reference; used to attribute device work). */
+unsigned long long wotg_launch_count(void);
+
+/* Squared-Euclidean cost |x_i - y_j|^2 between FP32 points (I x d, J x d, row
+ * strides ldx, ldy floats), written as an FP32 I x ldc matrix with +INF padding.
+ * Replaces sklearn pairwise_distances(metric='sqeuclidean') at
+ * wot/ot/ot_model.py:249-251 (coordinates already multiplied by the singular
+ * values, ot_model.py:245-247). */
+int wotg_cost_sqeuclidean(const float* X, int64_t I, int64_t ldx,
+                          const float* Y, int64_t J, int64_t ldy, int32_t d,
+                          float* C, int64_t ldc, void* stream);
+
+/* Dense FP64 cost (row-major, I x J, as the reference's C) -> FP32 I x ldc with
+ * +INF padding. Replaces np.asarray(C, dtype=np.float64) at
+ * wot/ot/optimal_transport.py:100 for user-supplied cost matrices. */
+int wotg_cost_from_f64(const double* C64, int64_t I, int64_t J, float* C, int64_t ldc,
+                       void* stream);
+
+/* np.median of the I x J valid entries of C (mean of the two middle values when
+ * I*J is even), exact on the FP32 values, result in FP64 on the HOST.
+ * Replaces np.median at wot/ot/ot_model.py:252. */
+size_t wotg_median_workspace_bytes(void);
+int wotg_median(const float* C, int64_t I, int64_t J, int64_t ldc, double* median_out,
+                void* workspace, size_t workspace_bytes, void* stream);
+
+/* Growth-iteration driver + solver: wot.ot.compute_transport_matrix
+ * (wot/ot/optimal_transport.py:10-33) with solver = params->solver.
+ * Outputs (device, any may be NULL):
+ *   tmap            I x J FP64 row-major, the coupling the reference returns
+ *                   (R / J, or R without / J when max_iter was hit)
+ *   learned_growth  growth_iters x I FP64, the reference's learned_growth list
+ *   row_sums        I FP64, tmap.sum(axis=1) of the returned coupling
+ *                   (appended by OTModel, ot_model.py:319)
+ *   u_bar, v_bar    I and J FP64 absorbed log-potentials (u + eps log a,
+ *                   v + eps log b) of the last solve, so that
+ *                   tmap = exp((u_bar_i + v_bar_j - cost_scale C_ij) / eps) / J
+ *                   with eps = stats->final_epsilon.
+ * stats (host) may be NULL. */
+size_t wotg_solve_workspace_bytes(int64_t I, int64_t J, int64_t ldc);
+int wotg_compute_transport_matrix(const wotg_problem* problem, const wotg_params* params,
+                                  double* tmap, double* learned_growth, double* row_sums,
+                                  double* u_bar, double* v_bar, wotg_stats* stats,
+                                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* One stabilised Sinkhorn half-step in the log domain, base 2:
+ *   axis 0:  L[i] = ln2 * log2 sum_j 2^(w[j] - kappa2 C_ij)   (w: ldc floats, padding 0)
+ *   axis 1:  L[j] = ln2 * log2 sum_i 2^(w[i] - kappa2 C_ij)   (w: I floats)
+ * i.e. log(K v) and log(K^T u) of the reference's K.dot(b * dy) / K.T.dot(a * dx)
+ * (wot/ot/optimal_transport.py:133-134) with K, a, b folded into w and C.
+ * axis 1 needs wotg_lse_matvec_workspace_bytes() of workspace; axis 0 none. */
+size_t wotg_lse_matvec_workspace_bytes(int64_t I, int64_t J, int64_t ldc);
+int wotg_lse_matvec(const float* C, int64_t I, int64_t J, int64_t ldc, const float* w, float kappa2,
+                    int32_t axis, double* L, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Dense population transport through one FP64 coupling X (I x J, row-major):
+ *   transpose == 0:  out (k x J) = P (k x I) @ X      push_forward, transport_map_model.py:290
+ *   transpose == 1:  out (k x I) = (X @ P^T)^T        pull_back,    transport_map_model.py:356
+ * with optional per-row normalisation of out to sum 1 (:291-292, :357-358).
+ * P and out are row-major FP64 on the device. */
+int wotg_apply_coupling_f64(const double* X, int64_t I, int64_t J, const double* P, int32_t k,
+                            int32_t transpose, int32_t normalize, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WOTG_H */

@@ -1,0 +1,114 @@
+"""Host-side logic that needs no GPU: configuration parsing, populations,
+paths, containers, map files and the C-ABI library's exported symbols."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import wot_gb300
+from wot_gb300 import Population, _native, io as wio
+from wot_gb300.dataset import Dataset, Frame
+from wot_gb300.ot import parse_configuration, parse_parameter_file
+from wot_gb300.ot.device import make_params
+from wot_gb300.tmap import find_path, unique_timepoint
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    with open(os.path.join(ROOT, 'include', 'wotg.h')) as f:
+        text = f.read()
+    return sorted(set(re.findall(r'^\s*(?:const\s+)?\w[\w\s\*]*?\b(wotg_\w+)\s*\(', text, flags=re.M)))
+
+
+def test_header_and_binding_agree():
+    assert header_symbols() == sorted(_native.EXPORTS)
+
+
+def test_library_loads_and_exports_everything():
+    from wot_gb300 import _build
+    _build.build()
+    lib = _native.load()
+    for name in header_symbols():
+        assert hasattr(lib, name), name
+    assert lib.wotg_version().decode().startswith('wotg')
+    assert lib.wotg_median_workspace_bytes() >= 4096 * 8
+
+
+def test_params_mapping_and_tau_none():
+    p = make_params({'epsilon': 0.01, 'lambda1': 3, 'growth_iters': 2, 'max_iter': 1e7}, 0)
+    assert p.epsilon == 0.01 and p.lambda1 == 3.0 and p.lambda2 == 50.0 and p.growth_iters == 2
+    assert p.batch_size == 5 and p.tolerance == 1e-8
+    with pytest.raises(TypeError):
+        make_params({'tau': None}, 1)
+
+
+def test_parse_configuration(tmp_path):
+    assert parse_configuration(None) is None
+    cfg = parse_configuration.__globals__['parse_per_timepair_configuration'](
+        {(0, 1): {'epsilon': 0.1, 'lambda1': 2, 'junk': 5}})
+    assert cfg == {(0, 1): {'epsilon': 0.1, 'lambda1': 2}}
+    with pytest.raises(ValueError):
+        parse_configuration({(0, 1): {}})
+    f = tmp_path / 'pairs.txt'
+    f.write_text('t0\tt1\tepsilon\n0\t1\t0.1\n1\t2\t0.2\n')
+    pairs = parse_configuration(str(f))
+    assert pairs[(0, 1)] == {'epsilon': 0.1} and pairs[(1, 2)] == {'epsilon': 0.2}
+    pf = tmp_path / 'params.txt'
+    pf.write_text('epsilon\t0.02\nlambda1\t4\n')
+    assert parse_parameter_file(str(pf)) == {'epsilon': 0.02, 'lambda1': 4}
+
+
+def test_population_copy_and_other():
+    a = Population(1.0, [1.0, 0.0, 0.0, 2.0], 'a')
+    b = Population(1.0, [0.0, 3.0, 0.0, 0.0], 'b')
+    pops = Population.copy(a, b, normalize=False, add_missing=True)
+    assert [p.name for p in pops] == ['a', 'b', 'Other']
+    np.testing.assert_array_equal(pops[0].p, [1, 0, 0, 1])
+    np.testing.assert_array_equal(pops[2].p, [0, 0, 1, 0])
+    pops = Population.copy(a, normalize=True)
+    assert pops[0].p.sum() == pytest.approx(1.0)
+    pops = Population.copy(a)
+    np.testing.assert_array_equal(pops[0].p, a.p)
+    assert unique_timepoint(a, b) == 1.0
+    with pytest.raises(ValueError):
+        unique_timepoint(a, Population(2.0, [1.0]))
+
+
+def test_find_path():
+    tp = [0, 1, 2, 3, 4]
+    assert find_path(0, 3, None, tp) == [(0, 1), (1, 2), (2, 3)]
+    assert find_path(0, 4, [(0, 2), (2, 4), (0, 1), (1, 2)], tp) == [(0, 1), (1, 2), (2, 4)]
+    with pytest.raises(ValueError):
+        find_path(0, 3, [(0, 1), (1, 2)], tp)
+
+
+def test_dataset_selection():
+    ds = Dataset(np.arange(12.).reshape(4, 3), Frame({'day': [0., 0., 1., 1.]}, index=['a', 'b', 'c', 'd']))
+    sub = ds[np.array([False, True, True, False]), :]
+    assert sub.shape == (2, 3) and list(sub.obs.index) == ['b', 'c']
+    np.testing.assert_array_equal(sub.X, [[3, 4, 5], [6, 7, 8]])
+
+
+def test_map_file_roundtrip(tmp_path):
+    ds = Dataset(np.random.default_rng(0).random((3, 4)), Frame({'g0': [1., 2., 3.]}, index=['x', 'y', 'z']),
+                 Frame(index=['p', 'q', 'r', 's']))
+    path = wio.check_file_extension(str(tmp_path / 'tmaps_1_2'), 'npz')
+    wio.write_dataset(ds, path, output_format='npz')
+    back = wio.read_dataset(path)
+    np.testing.assert_array_equal(back.X, ds.X)
+    assert list(back.obs.index) == ['x', 'y', 'z'] and list(back.var.index) == ['p', 'q', 'r', 's']
+    np.testing.assert_array_equal(back.obs['g0'], [1., 2., 3.])
+    m = wot_gb300.TransportMapModel.from_directory(str(tmp_path / 'tmaps'))
+    assert m.timepoints == [1.0, 2.0] and (1.0, 2.0) in m.tmaps
+    assert list(m.meta.index) == ['x', 'y', 'z', 'p', 'q', 'r', 's']
+
+
+def test_no_cpu_fallback_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip('a GPU is present')
+    with pytest.raises(RuntimeError, match='CUDA device'):
+        wot_gb300.ot.optimal_transport_duality_gap(np.zeros((2, 2)), np.ones(2), 1, 50, 0.05, 5, 1e-8, 1e4, 1, 1e7)

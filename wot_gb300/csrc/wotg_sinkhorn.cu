@@ -1,0 +1,884 @@
+// wotg_sinkhorn.cu — stabilised unbalanced Sinkhorn on a materialised FP32 cost (sm_103a).
+//
+// Reference: wot/ot/optimal_transport.py (wot 1.0.8)
+//   compute_transport_matrix        :10-33   -> wotg_compute_transport_matrix (growth loop)
+//   optimal_transport_duality_gap   :67-164  -> solve_duality_gap
+//   transport_stablev2              :167-236 -> solve_fixed_iters
+//   primal / dual                   :45-62   -> gap_partial_kernel (O(I+J), see below)
+//
+// State. The reference keeps FP64 absorbed potentials u, v, scalings a, b and
+// the stabilised kernel K = exp((u_i - C_ij + v_j)/eps) as a dense matrix that
+// it rebuilds at every absorption and epsilon change. Here the dense object is
+// the FP32 cost C (written once per day pair) and the scalings are kept in the
+// log domain (la = log a, lb = log b, FP64), so one half-step is
+//   log(K (b dy))_i = u_i/eps + log sum_j exp(v_j/eps + lb_j - cost_scale C_ij/eps) - log J
+// evaluated as a streaming base-2 log-sum-exp over the row of C, followed by the
+// reference's update a = (p / K(b dy))^alpha1 exp(-u/(lambda1+eps)) in FP64.
+// Absorption (u += eps log a, a = 1) then only touches O(I+J) vectors and no
+// matrix is ever rebuilt; the sequence of (u, v, a, b) is the reference's.
+//
+// Duality gap. With R = diag(a) K diag(b) the identity
+//   eps R_ij log R_ij + R_ij C_ij = R_ij (ubar_i + vbar_j),  ubar = u + eps log a,
+// turns the reference's primal - dual (two I x J passes with log) into sums over
+// the row sums x = R dy and column sums y = R^T dx only:
+//   primal - dual = F1(x) + F2(y) + F1*(-eps log a~) + F2*(-eps log b~) + dx<ubar,x> + dy<vbar,y>
+// (a~ = a exp(u/eps) evaluated as the reference does, overflow included), and
+//   primal = F1(x) + F2(y) + dx<ubar,x> + dy<vbar,y> + eps (sum(exp(-C/eps))/(IJ) - dx sum x).
+// The row sums with the current b are exactly the next iteration's first
+// half-step, so a gap check costs one row pass that the next iteration reuses.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "wotg_common.cuh"
+
+namespace wotg {
+
+// Per-solve vectors in the caller's workspace.
+struct Vecs {
+  double* u;       // I   absorbed potential (reference u)
+  double* v;       // J
+  double* la;      // I   log a
+  double* lb;      // J   log b
+  double* la_old;  // I   log a at the start of the last iteration (stage-exit test)
+  double* lb_old;  // J
+  double* logp;    // I   log p (p = G of this growth iteration)
+  double* p;       // I
+  double* Lrow;    // I   log sum_j exp(v_j/eps + lb_j - kappa C_ij)
+  double* Lcol;    // J   log sum_i exp(u_i/eps + la_i - kappa C_ij)
+  float* wrow;     // I   (u_i/eps + la_i) * log2(e), FP32 operand of the column pass
+  float* wcol;     // ldc (v_j/eps + lb_j) * log2(e), zero in padding columns
+  float2* part;    // nrb x ldc column-pass partials (m, s) in base 2
+  unsigned long long* maxslot;  // 2 slots of max(a, b) bits, alternating per iteration
+  double* red;     // kRedBlocks x kNq reduction partials
+  double* scal;    // kNq final sums + misc scalars
+  int* counters;   // [0] absorptions
+};
+
+constexpr int kNq = 8;
+constexpr int kRedBlocks = 296;
+
+struct Coef {
+  double eps, inv_eps;
+  double alpha1, alpha2;
+  double inv_l1e, inv_l2e;  // 1/(lambda + eps)
+  double lambda1, lambda2;
+  double logI, logJ, logq, q;
+  float kappa2;             // cost_scale / eps * log2(e)
+};
+
+struct Geom {
+  int64_t I, J, ldc;
+  int row_grid;
+  int ncb, nrb;             // column-pass grid: column blocks x row blocks
+  int64_t rows_per;
+};
+
+__device__ __forceinline__ void a_update(int64_t i, double L, const Vecs& V, const Coef& c,
+                                         unsigned long long* slot) {
+  const double ui = V.u[i];
+  const double logs = ui * c.inv_eps + L - c.logJ;                 // log (K (b dy))_i
+  const double la_new = c.alpha1 * (V.logp[i] - logs) - ui * c.inv_l1e;
+  V.la_old[i] = V.la[i];
+  V.la[i] = la_new;
+  V.wrow[i] = (float)((ui * c.inv_eps + la_new) * kLog2e);
+  atomic_max_nonneg(slot, exp(la_new));
+}
+
+__device__ __forceinline__ void b_update(int64_t j, double L, const Vecs& V, const Coef& c,
+                                         unsigned long long* slot) {
+  const double vj = V.v[j];
+  const double logt = vj * c.inv_eps + L - c.logI;                 // log (K^T (a dx))_j
+  const double lb_new = c.alpha2 * (c.logq - logt) - vj * c.inv_l2e;
+  V.lb_old[j] = V.lb[j];
+  V.lb[j] = lb_new;
+  V.wcol[j] = (float)((vj * c.inv_eps + lb_new) * kLog2e);
+  atomic_max_nonneg(slot, exp(lb_new));
+}
+
+// Row pass: one warp per row, 128-bit streaming loads of C, online base-2 LSE.
+// UPDATE_A additionally applies the a-update to the row (first half-step).
+template <bool UPDATE_A>
+__global__ void __launch_bounds__(256) row_pass_kernel(const float* __restrict__ C, Geom g,
+                                                       Vecs V, Coef c, int parity) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t nv = g.ldc >> 2;
+  const float4* __restrict__ w4 = reinterpret_cast<const float4*>(V.wcol);
+  const float k2 = c.kappa2;
+  for (int64_t i = warp; i < g.I; i += nwarps) {
+    const float4* __restrict__ row = reinterpret_cast<const float4*>(C + i * g.ldc);
+    float m = kNegBig, s = 0.f;
+    int64_t k = lane;
+    for (; k + 96 < nv; k += 128) {
+      float4 cc[4], ww[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) cc[t] = ld_stream(row + k + 32 * t);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) ww[t] = __ldg(w4 + k + 32 * t);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const float x0 = fmaf(-k2, cc[t].x, ww[t].x);
+        const float x1 = fmaf(-k2, cc[t].y, ww[t].y);
+        const float x2 = fmaf(-k2, cc[t].z, ww[t].z);
+        const float x3 = fmaf(-k2, cc[t].w, ww[t].w);
+        const float mn = fmaxf(m, fmaxf(fmaxf(x0, x1), fmaxf(x2, x3)));
+        s = s * ex2(m - mn) + ((ex2(x0 - mn) + ex2(x1 - mn)) + (ex2(x2 - mn) + ex2(x3 - mn)));
+        m = mn;
+      }
+    }
+    for (; k < nv; k += 32) {
+      const float4 cc = ld_stream(row + k);
+      const float4 ww = __ldg(w4 + k);
+      const float x0 = fmaf(-k2, cc.x, ww.x);
+      const float x1 = fmaf(-k2, cc.y, ww.y);
+      const float x2 = fmaf(-k2, cc.z, ww.z);
+      const float x3 = fmaf(-k2, cc.w, ww.w);
+      const float mn = fmaxf(m, fmaxf(fmaxf(x0, x1), fmaxf(x2, x3)));
+      s = s * ex2(m - mn) + ((ex2(x0 - mn) + ex2(x1 - mn)) + (ex2(x2 - mn) + ex2(x3 - mn)));
+      m = mn;
+    }
+    warp_lse(m, s);
+    if (lane == 0) {
+      const double L = ((double)m + log2((double)s)) * kLn2;
+      V.Lrow[i] = L;
+      if (UPDATE_A) a_update(i, L, V, c, V.maxslot + parity);
+    }
+  }
+}
+
+// a-update from a cached row LSE (the row pass of the preceding gap check).
+__global__ void a_update_kernel(Geom g, Vecs V, Coef c, int parity) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.I;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a_update(i, V.Lrow[i], V, c, V.maxslot + parity);
+}
+
+// Column pass, phase 1: CTA = 1024 columns (float4 per thread) x rows_per rows;
+// writes one (m, s) base-2 LSE partial per column and row block.
+constexpr int kColRowChunk = 4;
+
+__global__ void __launch_bounds__(256) col_partial_kernel(const float* __restrict__ C, Geom g,
+                                                          Vecs V, Coef c) {
+  const int64_t c4 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nv = g.ldc >> 2;
+  const int64_t r0 = (int64_t)blockIdx.y * g.rows_per;
+  const int64_t r1 = min(g.I, r0 + g.rows_per);
+  if (c4 >= nv) return;
+  const float k2 = c.kappa2;
+  float m[4] = {kNegBig, kNegBig, kNegBig, kNegBig};
+  float s[4] = {0.f, 0.f, 0.f, 0.f};
+  int64_t i = r0;
+  for (; i + kColRowChunk <= r1; i += kColRowChunk) {
+    float4 cc[kColRowChunk];
+    float w[kColRowChunk];
+#pragma unroll
+    for (int t = 0; t < kColRowChunk; ++t) cc[t] = ld_stream(reinterpret_cast<const float4*>(C + (i + t) * g.ldc) + c4);
+#pragma unroll
+    for (int t = 0; t < kColRowChunk; ++t) w[t] = __ldg(V.wrow + i + t);
+    float x[4][kColRowChunk];
+#pragma unroll
+    for (int t = 0; t < kColRowChunk; ++t) {
+      x[0][t] = fmaf(-k2, cc[t].x, w[t]);
+      x[1][t] = fmaf(-k2, cc[t].y, w[t]);
+      x[2][t] = fmaf(-k2, cc[t].z, w[t]);
+      x[3][t] = fmaf(-k2, cc[t].w, w[t]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float mx = x[q][0];
+#pragma unroll
+      for (int t = 1; t < kColRowChunk; ++t) mx = fmaxf(mx, x[q][t]);
+      const float mn = fmaxf(m[q], mx);
+      float acc = s[q] * ex2(m[q] - mn);
+#pragma unroll
+      for (int t = 0; t < kColRowChunk; ++t) acc += ex2(x[q][t] - mn);
+      s[q] = acc;
+      m[q] = mn;
+    }
+  }
+  for (; i < r1; ++i) {
+    const float4 cc = ld_stream(reinterpret_cast<const float4*>(C + i * g.ldc) + c4);
+    const float w = __ldg(V.wrow + i);
+    const float xs[4] = {fmaf(-k2, cc.x, w), fmaf(-k2, cc.y, w), fmaf(-k2, cc.z, w), fmaf(-k2, cc.w, w)};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float mn = fmaxf(m[q], xs[q]);
+      s[q] = s[q] * ex2(m[q] - mn) + ex2(xs[q] - mn);
+      m[q] = mn;
+    }
+  }
+  float4* out = reinterpret_cast<float4*>(V.part + (int64_t)blockIdx.y * g.ldc + c4 * 4);
+  out[0] = make_float4(m[0], s[0], m[1], s[1]);
+  out[1] = make_float4(m[2], s[2], m[3], s[3]);
+}
+
+// Column pass, phase 2: merge the row-block partials of each column in FP64,
+// then (UPDATE_B) the reference's b-update.
+template <bool UPDATE_B>
+__global__ void col_combine_kernel(Geom g, Vecs V, Coef c, int parity) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= g.J) return;
+  float mx = kNegBig;
+  for (int r = 0; r < g.nrb; ++r) mx = fmaxf(mx, V.part[(int64_t)r * g.ldc + j].x);
+  double s = 0.0;
+  for (int r = 0; r < g.nrb; ++r) {
+    const float2 ps = V.part[(int64_t)r * g.ldc + j];
+    s += (double)ps.y * (double)ex2(ps.x - mx);
+  }
+  const double L = ((double)mx + log2(s)) * kLn2;
+  V.Lcol[j] = L;
+  if (UPDATE_B) b_update(j, L, V, c, V.maxslot + parity);
+}
+
+// tau-absorption (optimal_transport.py:137-141 / :211-216): if max(a, b) > tau,
+// u += eps log a, v += eps log b, a = b = 1. Also clears the other max slot.
+__global__ void absorb_kernel(Geom g, Vecs V, Coef c, double tau, int parity) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const double mx = __longlong_as_double((long long)V.maxslot[parity]);
+  if (idx == 0) V.maxslot[parity ^ 1] = 0ull;
+  if (!(mx > tau)) return;
+  if (idx == 0) V.counters[0] += 1;
+  if (idx < g.I) {
+    const double un = V.u[idx] + c.eps * V.la[idx];
+    V.u[idx] = un;
+    V.la[idx] = 0.0;
+    V.wrow[idx] = (float)(un * c.inv_eps * kLog2e);
+  } else if (idx < g.I + g.J) {
+    const int64_t j = idx - g.I;
+    const double vn = V.v[j] + c.eps * V.lb[j];
+    V.v[j] = vn;
+    V.lb[j] = 0.0;
+    V.wcol[j] = (float)(vn * c.inv_eps * kLog2e);
+  }
+}
+
+// Absorb with the old epsilon, switch to the new one, reset a = b = 1
+// (stage start, optimal_transport.py:118-125; epsilon step, :218-228).
+__global__ void rescale_kernel(Geom g, Vecs V, double eps_old, double inv_eps_new) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx == 0) {
+    V.maxslot[0] = 0ull;
+    V.maxslot[1] = 0ull;
+  }
+  if (idx < g.I) {
+    const double un = V.u[idx] + eps_old * V.la[idx];
+    V.u[idx] = un;
+    V.la[idx] = 0.0;
+    V.la_old[idx] = 0.0;
+    V.wrow[idx] = (float)(un * inv_eps_new * kLog2e);
+  } else if (idx < g.I + g.J) {
+    const int64_t j = idx - g.I;
+    const double vn = V.v[j] + eps_old * V.lb[j];
+    V.v[j] = vn;
+    V.lb[j] = 0.0;
+    V.lb_old[j] = 0.0;
+    V.wcol[j] = (float)(vn * inv_eps_new * kLog2e);
+  }
+}
+
+// Zero state for a new solve; p = G; padding of wcol = 0.
+__global__ void init_kernel(Geom g, Vecs V, const double* __restrict__ G) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx == 0) {
+    V.maxslot[0] = 0ull;
+    V.maxslot[1] = 0ull;
+    V.counters[0] = 0;
+  }
+  if (idx < g.I) {
+    V.u[idx] = 0.0;
+    V.la[idx] = 0.0;
+    V.la_old[idx] = 0.0;
+    const double pi = G[idx];
+    V.p[idx] = pi;
+    V.logp[idx] = log(pi);
+    V.wrow[idx] = 0.f;
+  }
+  if (idx < g.ldc) {
+    V.wcol[idx] = 0.f;
+    if (idx < g.J) {
+      V.v[idx] = 0.0;
+      V.lb[idx] = 0.0;
+      V.lb_old[idx] = 0.0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic two-level FP64 reductions: kRedBlocks blocks write partials,
+// one block sums them.
+// ---------------------------------------------------------------------------
+template <int NQ>
+__device__ __forceinline__ void block_reduce_store(double (&acc)[NQ], double* out) {
+  __shared__ double sh[32][NQ];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) acc[q] = warp_sum(acc[q]);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) sh[wid][q] = acc[q];
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      double t = lane < nw ? sh[lane][q] : 0.0;
+      t = warp_sum(t);
+      if (lane == 0) out[q] = t;
+    }
+  }
+}
+
+__global__ void finalize_kernel(const double* __restrict__ red, int nblocks, double* out) {
+  double acc[kNq];
+#pragma unroll
+  for (int q = 0; q < kNq; ++q) acc[q] = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+#pragma unroll
+    for (int q = 0; q < kNq; ++q) acc[q] += red[b * kNq + q];
+  block_reduce_store<kNq>(acc, out);
+}
+
+// sum_ij exp(-kappa C_ij) over valid entries (the reference's sum of _K, used
+// in the primal objective at the final stage).
+__global__ void __launch_bounds__(256) sum_exp_kernel(const float* __restrict__ C, Geom g, float kappa2,
+                                                      double* red) {
+  const int64_t nv = g.ldc >> 2;
+  double acc[kNq];
+#pragma unroll
+  for (int q = 0; q < kNq; ++q) acc[q] = 0.0;
+  for (int64_t i = blockIdx.x; i < g.I; i += gridDim.x) {
+    const float4* row = reinterpret_cast<const float4*>(C + i * g.ldc);
+    float s = 0.f;
+    for (int64_t k = threadIdx.x; k < nv; k += blockDim.x) {
+      const float4 cc = ld_stream(row + k);
+      s += (ex2(-kappa2 * cc.x) + ex2(-kappa2 * cc.y)) + (ex2(-kappa2 * cc.z) + ex2(-kappa2 * cc.w));
+    }
+    acc[0] += (double)s;  // padding is +inf -> exp2(-inf) = 0
+  }
+  block_reduce_store<kNq>(acc, red + blockIdx.x * kNq);
+}
+
+// mean(G) (q = ones(J) * np.average(G), optimal_transport.py:108 / :192).
+__global__ void sum_vec_kernel(const double* __restrict__ x, int64_t n, double* red) {
+  double acc[kNq];
+#pragma unroll
+  for (int q = 0; q < kNq; ++q) acc[q] = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc[0] += x[i];
+  block_reduce_store<kNq>(acc, red + blockIdx.x * kNq);
+}
+
+// Stage-exit test (optimal_transport.py:158-160), FP64, as the reference
+// evaluates it: a~ = a * exp(u/eps), old = old_a * exp(u/eps).
+//   acc[0] = |a~ - old|^2, acc[1] = |a~|^2, acc[2], acc[3] likewise for b.
+__global__ void stage_test_kernel(Geom g, Vecs V, Coef c, double* red) {
+  double acc[kNq];
+#pragma unroll
+  for (int q = 0; q < kNq; ++q) acc[q] = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.I; i += stride) {
+    const double e = exp(V.u[i] * c.inv_eps);
+    const double ta = exp(V.la[i]) * e;
+    const double d = ta - exp(V.la_old[i]) * e;
+    acc[0] += d * d;
+    acc[1] += ta * ta;
+  }
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.J; j += stride) {
+    const double e = exp(V.v[j] * c.inv_eps);
+    const double tb = exp(V.lb[j]) * e;
+    const double d = tb - exp(V.lb_old[j]) * e;
+    acc[2] += d * d;
+    acc[3] += tb * tb;
+  }
+  block_reduce_store<kNq>(acc, red + blockIdx.x * kNq);
+}
+
+// Duality-gap terms (final stage). Needs Lrow with the current b and Lcol
+// with the current a.
+//   acc[0] = sum_i [lambda1 (x log(x/p) - x + p) + lambda1 p (exp(-eps log a~/lambda1) - 1) + ubar x]
+//   acc[1] = same over j with lambda2, q, b~, vbar, y
+//   acc[2] = sum_i (x log(x/p) - x + p)       acc[3] = sum_j (y log(y/q) - y + q)
+//   acc[4] = sum_i ubar x                      acc[5] = sum_j vbar y
+//   acc[6] = sum_i x
+__global__ void gap_partial_kernel(Geom g, Vecs V, Coef c, double* red) {
+  double acc[kNq];
+#pragma unroll
+  for (int q = 0; q < kNq; ++q) acc[q] = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.I; i += stride) {
+    const double ui = V.u[i], lai = V.la[i], pi = V.p[i];
+    const double x = exp(lai + ui * c.inv_eps + V.Lrow[i] - c.logJ);
+    const double ub = ui + c.eps * lai;
+    const double at = exp(lai) * exp(ui * c.inv_eps);
+    const double f = x * log(x / pi) - x + pi;
+    const double conj = c.lambda1 * pi * (exp(-c.eps * log(at) / c.lambda1) - 1.0);
+    acc[0] += c.lambda1 * f + conj + ub * x;
+    acc[2] += f;
+    acc[4] += ub * x;
+    acc[6] += x;
+  }
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.J; j += stride) {
+    const double vj = V.v[j], lbj = V.lb[j];
+    const double y = exp(lbj + vj * c.inv_eps + V.Lcol[j] - c.logI);
+    const double vb = vj + c.eps * lbj;
+    const double bt = exp(lbj) * exp(vj * c.inv_eps);
+    const double f = y * log(y / c.q) - y + c.q;
+    const double conj = c.lambda2 * c.q * (exp(-c.eps * log(bt) / c.lambda2) - 1.0);
+    acc[1] += c.lambda2 * f + conj + vb * y;
+    acc[3] += f;
+    acc[5] += vb * y;
+  }
+  block_reduce_store<kNq>(acc, red + blockIdx.x * kNq);
+}
+
+// Outputs. `log_scale` is the log of the factor applied to R = diag(a) K diag(b):
+// -log J for the reference's normal return R / J, 0 for its max_iter return R.
+// Row sums of the returned coupling (tmap.sum(axis=1)); needs Lrow with the final b.
+__global__ void row_sums_kernel(Geom g, Vecs V, Coef c, double log_scale, double* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.I;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = exp(V.la[i] + V.u[i] * c.inv_eps + V.Lrow[i] + log_scale);
+}
+
+__global__ void potentials_kernel(Geom g, Vecs V, Coef c, double* __restrict__ ubar,
+                                  double* __restrict__ vbar) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < g.I) {
+    if (ubar) ubar[idx] = V.u[idx] + c.eps * V.la[idx];
+  } else if (idx < g.I + g.J) {
+    const int64_t j = idx - g.I;
+    if (vbar) vbar[j] = V.v[j] + c.eps * V.lb[j];
+  }
+}
+
+// Dense coupling tmap_ij = a_i exp((u_i - C_ij + v_j)/eps) b_j * exp(log_scale), written
+// FP64 row-major (stride J) like the reference's ndarray.
+__global__ void __launch_bounds__(256) coupling_kernel(const float* __restrict__ C, Geom g, Vecs V,
+                                                       Coef c, double log_scale, double* __restrict__ out) {
+  const float k2 = c.kappa2;
+  for (int64_t i = blockIdx.y; i < g.I; i += gridDim.y) {
+    const float wr = (float)((V.u[i] * c.inv_eps + V.la[i] + log_scale) * kLog2e);
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.J;
+         j += (int64_t)gridDim.x * blockDim.x) {
+      const float x = wr + V.wcol[j] - k2 * C[i * g.ldc + j];
+      out[i * g.J + j] = (double)ex2(x);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct Solver {
+  const float* C;
+  Geom g;
+  Vecs V;
+  cudaStream_t st;
+  double cost_scale;
+  int small_grid;  // grid for O(I+J) kernels
+
+  Coef coef(double eps, const wotg_params& P, double q) const {
+    Coef c;
+    c.eps = eps;
+    c.inv_eps = 1.0 / eps;
+    c.alpha1 = P.lambda1 / (P.lambda1 + eps);
+    c.alpha2 = P.lambda2 / (P.lambda2 + eps);
+    c.inv_l1e = 1.0 / (P.lambda1 + eps);
+    c.inv_l2e = 1.0 / (P.lambda2 + eps);
+    c.lambda1 = P.lambda1;
+    c.lambda2 = P.lambda2;
+    c.logI = std::log((double)g.I);
+    c.logJ = std::log((double)g.J);
+    c.q = q;
+    c.logq = std::log(q);
+    c.kappa2 = (float)(cost_scale / eps * kLog2e);
+    return c;
+  }
+
+  int vec_blocks(int64_t n) const { return (int)std::max<int64_t>(1, (n + 255) / 256); }
+
+  int iteration(const Coef& c, bool lrow_valid, int parity, bool update_b_only = false) {
+    (void)update_b_only;
+    if (lrow_valid) {
+      a_update_kernel<<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, parity);
+    } else {
+      row_pass_kernel<true><<<g.row_grid, 256, 0, st>>>(C, g, V, c, parity);
+    }
+    WOTG_LAUNCHED();
+    col_partial_kernel<<<dim3(g.ncb, g.nrb), 256, 0, st>>>(C, g, V, c);
+    WOTG_LAUNCHED();
+    col_combine_kernel<true><<<vec_blocks(g.J), 256, 0, st>>>(g, V, c, parity);
+    WOTG_LAUNCHED();
+    return WOTG_OK;
+  }
+
+  int absorb(const Coef& c, double tau, int parity) {
+    absorb_kernel<<<vec_blocks(g.I + g.J), 256, 0, st>>>(g, V, c, tau, parity);
+    WOTG_LAUNCHED();
+    return WOTG_OK;
+  }
+
+  int rescale(double eps_old, double eps_new) {
+    rescale_kernel<<<vec_blocks(g.I + g.J), 256, 0, st>>>(g, V, eps_old, 1.0 / eps_new);
+    WOTG_LAUNCHED();
+    return WOTG_OK;
+  }
+
+  int reduce_to_host(double* host8) {
+    finalize_kernel<<<1, 256, 0, st>>>(V.red, kRedBlocks, V.scal);
+    WOTG_LAUNCHED();
+    WOTG_CUDA(cudaMemcpyAsync(host8, V.scal, kNq * sizeof(double), cudaMemcpyDeviceToHost, st));
+    WOTG_CUDA(cudaStreamSynchronize(st));
+    return WOTG_OK;
+  }
+
+  int mean_of(const double* x, int64_t n, double* out) {
+    sum_vec_kernel<<<kRedBlocks, 256, 0, st>>>(x, n, V.red);
+    WOTG_LAUNCHED();
+    double h[kNq];
+    int s = reduce_to_host(h);
+    if (s) return s;
+    *out = h[0] / (double)n;
+    return WOTG_OK;
+  }
+
+  int sum_exp(const Coef& c, double* out) {
+    sum_exp_kernel<<<kRedBlocks, 256, 0, st>>>(C, g, c.kappa2, V.red);
+    WOTG_LAUNCHED();
+    double h[kNq];
+    int s = reduce_to_host(h);
+    if (s) return s;
+    *out = h[0];
+    return WOTG_OK;
+  }
+
+  int fresh_lrow(const Coef& c) {
+    row_pass_kernel<false><<<g.row_grid, 256, 0, st>>>(C, g, V, c, 0);
+    WOTG_LAUNCHED();
+    return WOTG_OK;
+  }
+
+  // Solver outputs for one solve: learned row sums (device), optionally the
+  // dense coupling and potentials.
+  int outputs(const Coef& c, bool no_div_j, double* tmap, double* row_sums, double* ubar,
+              double* vbar) {
+    const double log_scale = no_div_j ? 0.0 : -c.logJ;
+    if (row_sums) {
+      row_sums_kernel<<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, log_scale, row_sums);
+      WOTG_LAUNCHED();
+    }
+    if (ubar || vbar) {
+      potentials_kernel<<<vec_blocks(g.I + g.J), 256, 0, st>>>(g, V, c, ubar, vbar);
+      WOTG_LAUNCHED();
+    }
+    if (tmap) {
+      dim3 grid((unsigned)std::min<int64_t>((g.J + 255) / 256, 16), (unsigned)std::min<int64_t>(g.I, 65535));
+      coupling_kernel<<<grid, 256, 0, st>>>(C, g, V, c, log_scale, tmap);
+      WOTG_LAUNCHED();
+    }
+    return WOTG_OK;
+  }
+};
+
+struct SolveResult {
+  int status = WOTG_OK;
+  bool max_iter = false;
+  int64_t iterations = 0;
+  int64_t checks = 0;
+  double gap = NAN;
+  double eps = 0.0;
+  Coef final_coef{};
+};
+
+// Python's max(x, y): returns x unless y > x (so a NaN in first position wins).
+static inline double py_max(double x, double y) { return (y > x) ? y : x; }
+
+static int solve_duality_gap(Solver& S, const wotg_params& P, double q, SolveResult& res) {
+  const int n_scalings = 5;
+  const double scale_factor = std::exp(-std::log(P.epsilon) / n_scalings);
+  double eps_i = P.epsilon0 * scale_factor;
+  int64_t it = 0;
+  int parity = 0;
+  double gap = INFINITY;
+  Coef c{};
+  bool lrow_valid = false;
+  for (int stage = 0; stage <= n_scalings; ++stage) {
+    gap = INFINITY;
+    const double eps_old = eps_i;
+    eps_i = eps_i / scale_factor;
+    c = S.coef(eps_i, P, q);
+    int s = S.rescale(eps_old, eps_i);
+    if (s) return s;
+    parity = 0;
+    lrow_valid = false;
+    const bool final = stage == n_scalings;
+    const double threshold = final ? P.tolerance : 1e-6;
+    double sumK = 0.0;
+    if (final) {
+      s = S.sum_exp(c, &sumK);
+      if (s) return s;
+    }
+    while (gap > threshold) {
+      const int nb = final ? P.batch_size : 5;
+      for (int t = 0; t < nb; ++t) {
+        ++it;
+        s = S.iteration(c, lrow_valid, parity);
+        if (s) return s;
+        lrow_valid = false;
+        s = S.absorb(c, P.tau, parity);
+        if (s) return s;
+        parity ^= 1;
+        if ((double)it >= P.max_iter) {
+          res.max_iter = true;
+          res.iterations = it;
+          res.gap = gap;
+          res.eps = eps_i;
+          res.final_coef = c;
+          s = S.fresh_lrow(c);
+          if (s) return s;
+          return WOTG_OK;
+        }
+      }
+      double h[kNq];
+      ++res.checks;
+      if (final) {
+        s = S.fresh_lrow(c);
+        if (s) return s;
+        lrow_valid = true;
+        gap_partial_kernel<<<kRedBlocks, 256, 0, S.st>>>(S.g, S.V, c, S.V.red);
+        WOTG_LAUNCHED();
+        s = S.reduce_to_host(h);
+        if (s) return s;
+        const double I = (double)S.g.I, J = (double)S.g.J;
+        const double dx = 1.0 / I, dy = 1.0 / J;
+        const double gap_abs = dx * h[0] + dy * h[1];
+        const double pri = P.lambda1 * dx * h[2] + P.lambda2 * dy * h[3] + dx * h[4] + dy * h[5] +
+                           eps_i * (sumK / (I * J) - dx * h[6]);
+        gap = gap_abs / std::fabs(pri);
+      } else {
+        stage_test_kernel<<<kRedBlocks, 256, 0, S.st>>>(S.g, S.V, c, S.V.red);
+        WOTG_LAUNCHED();
+        s = S.reduce_to_host(h);
+        if (s) return s;
+        const double ga = std::sqrt(h[0]) / (1.0 + std::sqrt(h[1]));
+        const double gb = std::sqrt(h[2]) / (1.0 + std::sqrt(h[3]));
+        gap = py_max(ga, gb);
+      }
+    }
+  }
+  res.iterations = it;
+  res.gap = gap;
+  res.eps = eps_i;
+  res.final_coef = c;
+  if (std::isnan(gap)) return WOTG_NONFINITE;
+  // Lrow is valid (last gap check ran with the current b).
+  return WOTG_OK;
+}
+
+static int solve_fixed_iters(Solver& S, const wotg_params& P, double q, SolveResult& res) {
+  const double eps_final = P.epsilon;
+  double eps_i = P.epsilon0;  // tau is never None here (the host rejects it)
+  Coef c = S.coef(eps_i, P, q);
+  int s = S.rescale(0.0, eps_i);
+  if (s) return s;
+  int parity = 0;
+  int since = 0, index = 0;
+  for (int it = 0; it < P.scaling_iter; ++it) {
+    s = S.iteration(c, false, parity);
+    if (s) return s;
+    ++since;
+    s = S.absorb(c, P.tau, parity);
+    if (s) return s;
+    parity ^= 1;
+    if (since == P.inner_iter_max) {
+      ++index;
+      since = 0;
+      const double eps_new = (P.epsilon0 - eps_final) * std::exp(-(double)index) + eps_final;
+      s = S.rescale(eps_i, eps_new);
+      if (s) return s;
+      parity = 0;
+      eps_i = eps_new;
+      c = S.coef(eps_i, P, q);
+    }
+  }
+  for (int it = 0; it < P.extra_iter; ++it) {
+    s = S.iteration(c, false, parity);
+    if (s) return s;
+  }
+  s = S.fresh_lrow(c);
+  if (s) return s;
+  res.iterations = (int64_t)P.scaling_iter + P.extra_iter;
+  res.eps = eps_i;
+  res.final_coef = c;
+  return WOTG_OK;
+}
+
+static Geom make_geom(int64_t I, int64_t J, int64_t ldc) {
+  Geom g;
+  g.I = I;
+  g.J = J;
+  g.ldc = ldc;
+  const int sms = sm_count();
+  const int64_t max_warps = (int64_t)sms * 6 * 8;
+  const int64_t rows_per_warp = (I + max_warps - 1) / max_warps;
+  const int64_t warps = (I + rows_per_warp - 1) / rows_per_warp;
+  g.row_grid = (int)std::max<int64_t>(1, (warps + 7) / 8);
+  const int64_t nv = ldc >> 2;
+  g.ncb = (int)std::max<int64_t>(1, (nv + 255) / 256);
+  int64_t nrb = std::max<int64_t>(1, ((int64_t)sms * 6) / g.ncb);
+  nrb = std::min<int64_t>(nrb, std::max<int64_t>(1, I / 8));
+  int64_t rows_per = (I + nrb - 1) / nrb;
+  rows_per = (rows_per + kColRowChunk - 1) / kColRowChunk * kColRowChunk;
+  g.rows_per = rows_per;
+  g.nrb = (int)((I + rows_per - 1) / rows_per);
+  return g;
+}
+
+static size_t layout(Bump& b, const Geom& g, Vecs& V) {
+  V.u = b.take<double>(g.I);
+  V.la = b.take<double>(g.I);
+  V.la_old = b.take<double>(g.I);
+  V.logp = b.take<double>(g.I);
+  V.p = b.take<double>(g.I);
+  V.Lrow = b.take<double>(g.I);
+  V.v = b.take<double>(g.J);
+  V.lb = b.take<double>(g.J);
+  V.lb_old = b.take<double>(g.J);
+  V.Lcol = b.take<double>(g.J);
+  V.wrow = b.take<float>(g.I);
+  V.wcol = b.take<float>(g.ldc);
+  V.part = b.take<float2>((size_t)g.nrb * g.ldc);
+  V.maxslot = b.take<unsigned long long>(2);
+  V.red = b.take<double>((size_t)kRedBlocks * kNq);
+  V.scal = b.take<double>(16);
+  V.counters = b.take<int>(8);
+  V.scal = V.scal;
+  return b.off + 256;
+}
+
+}  // namespace wotg
+
+using namespace wotg;
+
+extern "C" size_t wotg_lse_matvec_workspace_bytes(int64_t I, int64_t J, int64_t ldc) {
+  if (I <= 0 || J <= 0 || ldc < J) return 0;
+  Geom g = make_geom(I, J, ldc);
+  return (size_t)g.nrb * (size_t)ldc * sizeof(float2) + 256;
+}
+
+extern "C" int wotg_lse_matvec(const float* C, int64_t I, int64_t J, int64_t ldc, const float* w, float kappa2,
+                               int32_t axis, double* L, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!C || !w || !L || I <= 0 || J <= 0 || ldc < J || (ldc & 3) || (axis != 0 && axis != 1)) return WOTG_BADARG;
+  if ((reinterpret_cast<uintptr_t>(C) & 15) || (axis == 0 && (reinterpret_cast<uintptr_t>(w) & 15)))
+    return WOTG_BADARG;
+  Geom g = make_geom(I, J, ldc);
+  Vecs V{};
+  Coef c{};
+  c.kappa2 = kappa2;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (axis == 0) {
+    V.wcol = const_cast<float*>(w);
+    V.Lrow = L;
+    row_pass_kernel<false><<<g.row_grid, 256, 0, st>>>(C, g, V, c, 0);
+    WOTG_LAUNCHED();
+    return WOTG_OK;
+  }
+  if (!workspace || workspace_bytes < wotg_lse_matvec_workspace_bytes(I, J, ldc)) return WOTG_WORKSPACE;
+  V.wrow = const_cast<float*>(w);
+  V.Lcol = L;
+  V.part = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  col_partial_kernel<<<dim3(g.ncb, g.nrb), 256, 0, st>>>(C, g, V, c);
+  WOTG_LAUNCHED();
+  col_combine_kernel<false><<<(unsigned)((J + 255) / 256), 256, 0, st>>>(g, V, c, 0);
+  WOTG_LAUNCHED();
+  return WOTG_OK;
+}
+
+extern "C" size_t wotg_solve_workspace_bytes(int64_t I, int64_t J, int64_t ldc) {
+  if (I <= 0 || J <= 0 || ldc < J) return 0;
+  Geom g = make_geom(I, J, ldc);
+  Bump b{nullptr, 0};
+  Vecs V{};
+  // extra I doubles: learned-growth carry between growth iterations
+  b.take<double>(I);
+  return layout(b, g, V);
+}
+
+extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wotg_params* params,
+                                             double* tmap, double* learned_growth, double* row_sums,
+                                             double* u_bar, double* v_bar, wotg_stats* stats,
+                                             void* workspace, size_t workspace_bytes, void* stream) {
+  if (!prob || !params) return WOTG_BADARG;
+  const wotg_params P = *params;
+  const int64_t I = prob->I, J = prob->J, ldc = prob->ldc;
+  if (I <= 0 || J <= 0 || ldc < J || (ldc & 3) || !prob->C || !prob->G) return WOTG_BADARG;
+  if ((reinterpret_cast<uintptr_t>(prob->C) & 15) != 0) return WOTG_BADARG;
+  if (!(P.epsilon > 0) || !(P.epsilon0 > 0) || P.growth_iters < 1) return WOTG_BADARG;
+  if (P.solver == WOTG_SOLVER_DUALITY_GAP) {
+    if (P.batch_size < 1) return WOTG_BADARG;
+  } else if (P.solver == WOTG_SOLVER_FIXED_ITERS) {
+    if (P.scaling_iter < 1 || P.extra_iter < 0) return WOTG_BADARG;
+  } else {
+    return WOTG_BADARG;
+  }
+  if (!workspace || workspace_bytes < wotg_solve_workspace_bytes(I, J, ldc)) return WOTG_WORKSPACE;
+
+  Geom g = make_geom(I, J, ldc);
+  // layout() leaves 256 bytes of slack for aligning the caller's base pointer
+  Bump b{reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255)), 0};
+  double* carry = b.take<double>(I);
+  Vecs V{};
+  layout(b, g, V);
+  cudaStream_t st = (cudaStream_t)stream;
+  Solver S{prob->C, g, V, st, prob->cost_scale, 0};
+
+  wotg_stats total{};
+  int status = WOTG_OK;
+  const double* G = prob->G;
+  for (int gi = 0; gi < P.growth_iters; ++gi) {
+    if (learned_growth) {
+      WOTG_CUDA(cudaMemcpyAsync(learned_growth + (int64_t)gi * I, G, I * sizeof(double),
+                                cudaMemcpyDeviceToDevice, st));
+    }
+    init_kernel<<<S.vec_blocks(std::max(I, ldc)), 256, 0, st>>>(g, V, G);
+    WOTG_LAUNCHED();
+    double q = 0.0;
+    int s = S.mean_of(V.p, I, &q);
+    if (s) return s;
+    SolveResult res;
+    s = (P.solver == WOTG_SOLVER_DUALITY_GAP) ? solve_duality_gap(S, P, q, res)
+                                              : solve_fixed_iters(S, P, q, res);
+    int absorptions = 0;
+    WOTG_CUDA(cudaMemcpyAsync(&absorptions, V.counters, sizeof(int), cudaMemcpyDeviceToHost, st));
+    WOTG_CUDA(cudaStreamSynchronize(st));
+    total.iterations += res.iterations;
+    total.absorptions += absorptions;
+    total.checks += res.checks;
+    total.gap = res.gap;
+    total.final_epsilon = res.eps;
+    if (s == WOTG_NONFINITE) {
+      status = WOTG_NONFINITE;
+      break;
+    }
+    if (s) return s;
+    if (res.max_iter) {
+      total.hit_max_iter = 1;
+      status = WOTG_MAX_ITER;
+    }
+    const bool last = gi == P.growth_iters - 1;
+    if (!last) {
+      s = S.outputs(res.final_coef, res.max_iter, nullptr, carry, nullptr, nullptr);
+      if (s) return s;
+      G = carry;
+    } else {
+      s = S.outputs(res.final_coef, res.max_iter, tmap, row_sums, u_bar, v_bar);
+      if (s) return s;
+    }
+  }
+  WOTG_CUDA(cudaStreamSynchronize(st));
+  if (stats) *stats = total;
+  return status;
+}

@@ -1,0 +1,180 @@
+"""Device-level API over libwotg: costs, median, solves and population transport.
+
+Buffers are torch tensors on the current CUDA device (torch is used for device
+memory and streams only); every computation is a libwotg kernel launched on
+``torch.cuda.current_stream()``.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .. import _native as N
+
+# The reference's solver keys (ot_model.py:85-87) and their C types.
+_PARAM_KEYS = ('epsilon', 'lambda1', 'lambda2', 'epsilon0', 'tau', 'tolerance', 'max_iter',
+               'batch_size', 'scaling_iter', 'inner_iter_max', 'extra_iter', 'growth_iters')
+DEFAULTS = {'growth_iters': 1, 'epsilon': 0.05, 'lambda1': 1, 'lambda2': 50, 'epsilon0': 1, 'tau': 10000,
+            'scaling_iter': 3000, 'inner_iter_max': 50, 'tolerance': 1e-8, 'max_iter': 1e7,
+            'batch_size': 5, 'extra_iter': 1000}
+
+
+@dataclass
+class DeviceCost:
+    """FP32 cost on the device, I x ldc with +inf padding; reference cost = scale * C."""
+    C: object
+    I: int
+    J: int
+    ldc: int
+    scale: float = 1.0
+
+    @property
+    def shape(self):
+        return (self.I, self.J)
+
+
+@dataclass
+class SolveResult:
+    tmap: object = None            # I x J FP64 device tensor (or None)
+    learned_growth: list = field(default_factory=list)   # growth_iters device tensors of I
+    row_sums: object = None        # tmap.sum(axis=1)
+    u_bar: object = None
+    v_bar: object = None
+    stats: dict = field(default_factory=dict)
+    status: int = 0
+
+
+def _torch():
+    return N.require_cuda()
+
+
+def _stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dev_f64(x, torch):
+    if isinstance(x, torch.Tensor):
+        return x.to(device='cuda', dtype=torch.float64).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(np.asarray(x, dtype=np.float64)), device='cuda')
+
+
+def _dev_f32(x, torch):
+    if isinstance(x, torch.Tensor):
+        return x.to(device='cuda', dtype=torch.float32).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(np.asarray(x, dtype=np.float32)), device='cuda')
+
+
+def cost_from_dense(C) -> DeviceCost:
+    """User-supplied dense cost (reference's C, FP64) -> FP32 device cost, scale 1."""
+    torch = _torch()
+    C64 = _dev_f64(C, torch)
+    if C64.dim() != 2:
+        raise ValueError('cost matrix must be 2-D')
+    I, J = C64.shape
+    ldc = N.round_up(J, 4)
+    C32 = torch.empty((I, ldc), dtype=torch.float32, device='cuda')
+    N.check(N.load().wotg_cost_from_f64(C64.data_ptr(), I, J, C32.data_ptr(), ldc, _stream()),
+            'wotg_cost_from_f64')
+    return DeviceCost(C32, I, J, ldc, 1.0)
+
+
+def cost_from_points(x, y) -> DeviceCost:
+    """Squared-Euclidean FP32 cost between point sets (rows), unnormalised (scale 1)."""
+    torch = _torch()
+    X = _dev_f32(x, torch)
+    Y = _dev_f32(y, torch)
+    if X.dim() != 2 or Y.dim() != 2 or X.shape[1] != Y.shape[1]:
+        raise ValueError('points must be 2-D with the same dimension')
+    I, d = X.shape
+    J = Y.shape[0]
+    ldc = N.round_up(J, 4)
+    C32 = torch.empty((I, ldc), dtype=torch.float32, device='cuda')
+    N.check(N.load().wotg_cost_sqeuclidean(X.data_ptr(), I, X.stride(0), Y.data_ptr(), J, Y.stride(0), d,
+                                           C32.data_ptr(), ldc, _stream()), 'wotg_cost_sqeuclidean')
+    return DeviceCost(C32, I, J, ldc, 1.0)
+
+
+def median(cost: DeviceCost) -> float:
+    """np.median of the valid FP32 cost entries (exact on the FP32 values)."""
+    torch = _torch()
+    lib = N.load()
+    ws = torch.empty(lib.wotg_median_workspace_bytes(), dtype=torch.uint8, device='cuda')
+    out = ctypes.c_double(0.0)
+    N.check(lib.wotg_median(cost.C.data_ptr(), cost.I, cost.J, cost.ldc, ctypes.byref(out), ws.data_ptr(),
+                            ws.numel(), _stream()), 'wotg_median')
+    return out.value
+
+
+def default_cost(x, y) -> DeviceCost:
+    """Median-normalised squared-Euclidean cost (wot/ot/ot_model.py:242-253)."""
+    c = cost_from_points(x, y)
+    med = median(c)
+    c.scale = 1.0 / med
+    return c
+
+
+def make_params(cfg: dict, solver: int) -> N.Params:
+    p = dict(DEFAULTS)
+    p.update({k: cfg[k] for k in _PARAM_KEYS if k in cfg and cfg[k] is not None})
+    if cfg.get('tau', 0) is None:
+        # the reference compares max(...) > None, which Python 3 rejects
+        raise TypeError("'>' not supported between instances of 'numpy.float64' and 'NoneType'")
+    return N.Params(epsilon=float(p['epsilon']), lambda1=float(p['lambda1']), lambda2=float(p['lambda2']),
+                    epsilon0=float(p['epsilon0']), tau=float(p['tau']), tolerance=float(p['tolerance']),
+                    max_iter=float(p['max_iter']), batch_size=int(p['batch_size']),
+                    scaling_iter=int(p['scaling_iter']), inner_iter_max=int(p['inner_iter_max']),
+                    extra_iter=int(p['extra_iter']), growth_iters=int(p['growth_iters']), solver=int(solver))
+
+
+def solve(cost: DeviceCost, G, cfg: dict, solver: int = N.SOLVER_DUALITY_GAP, want_tmap: bool = True,
+          want_potentials: bool = False, tmap_out=None) -> SolveResult:
+    """All growth iterations of one transport problem on the device
+    (wot.ot.compute_transport_matrix, optimal_transport.py:10-33)."""
+    torch = _torch()
+    lib = N.load()
+    params = make_params(cfg, solver)
+    I, J = cost.I, cost.J
+    Gd = _dev_f64(G, torch).reshape(-1)
+    if Gd.numel() != I:
+        raise ValueError('G has %d entries for %d source cells' % (Gd.numel(), I))
+    gi = max(1, params.growth_iters)
+    learned = torch.empty((gi, I), dtype=torch.float64, device='cuda')
+    row_sums = torch.empty(I, dtype=torch.float64, device='cuda')
+    tmap = None
+    if want_tmap:
+        tmap = tmap_out if tmap_out is not None else torch.empty((I, J), dtype=torch.float64, device='cuda')
+    u_bar = torch.empty(I, dtype=torch.float64, device='cuda') if want_potentials else None
+    v_bar = torch.empty(J, dtype=torch.float64, device='cuda') if want_potentials else None
+    nbytes = lib.wotg_solve_workspace_bytes(I, J, cost.ldc)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
+    prob = N.Problem(I=I, J=J, C=cost.C.data_ptr(), ldc=cost.ldc, cost_scale=float(cost.scale),
+                     G=Gd.data_ptr())
+    stats = N.Stats()
+    status = lib.wotg_compute_transport_matrix(ctypes.byref(prob), ctypes.byref(params), N.ptr(tmap),
+                                               learned.data_ptr(), row_sums.data_ptr(), N.ptr(u_bar),
+                                               N.ptr(v_bar), ctypes.byref(stats), ws.data_ptr(), nbytes,
+                                               _stream())
+    N.check(status, 'wotg_compute_transport_matrix')
+    return SolveResult(tmap=tmap, learned_growth=[learned[k] for k in range(gi)], row_sums=row_sums,
+                       u_bar=u_bar, v_bar=v_bar, stats=stats.as_dict(), status=status)
+
+
+def apply_coupling(X, P, transpose: bool, normalize: bool):
+    """push (transpose=False): P @ X; pull (transpose=True): (X @ P.T).T; FP64 on device."""
+    torch = _torch()
+    Xd = _dev_f64(X, torch)
+    Pd = _dev_f64(P, torch)
+    if Pd.dim() == 1:
+        Pd = Pd.reshape(1, -1)
+    I, J = Xd.shape
+    k = Pd.shape[0]
+    if Pd.shape[1] != (J if transpose else I):
+        raise ValueError('population length %d does not match the coupling %s' % (Pd.shape[1], (I, J)))
+    out = torch.empty((k, I if transpose else J), dtype=torch.float64, device='cuda')
+    N.check(N.load().wotg_apply_coupling_f64(Xd.data_ptr(), I, J, Pd.data_ptr(), k, int(transpose),
+                                             int(normalize), out.data_ptr(), _stream()),
+            'wotg_apply_coupling_f64')
+    return out
