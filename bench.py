@@ -44,6 +44,7 @@ def parse():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--pair', default=None, help='I,J cells of a smaller pair (profiling runs)')
     ap.add_argument('--no-cpu', action='store_true')
     return ap.parse_args()
 
@@ -108,9 +109,10 @@ class Clocks:
                 'samples': len(sm)}
 
 
-def make_pair(seed, I=I_FULL, J=J_FULL):
+def make_pair(seed, I=None, J=None):
     from wot_gb300 import synthetic
-    X, day, growth = synthetic.time_course([I, J], n_genes=GENES, n_clusters=CLUSTERS, seed=seed)
+    X, day, growth = synthetic.time_course([I or I_FULL, J or J_FULL], n_genes=GENES, n_clusters=CLUSTERS,
+                                           seed=seed)
     return X, day, growth
 
 
@@ -186,7 +188,11 @@ def run_reference(args):
 
 
 def main():
+    global I_FULL, J_FULL, WORKLOAD
     args = parse()
+    if args.pair:
+        I_FULL, J_FULL = (int(v) for v in args.pair.split(','))
+        WORKLOAD = WORKLOAD.replace('20000x25000', '%dx%d' % (I_FULL, J_FULL))
     if args.impl == 'reference':
         run_reference(args)
         return
