@@ -5,8 +5,9 @@ The reference stacks both days' cells, removes the per-gene mean, and fits
 genes are the samples and cells the features; the cell coordinates are the
 rows of ``components_.T`` and ``singular_values_`` scale them in the cost.
 Here the same double-centred matrix is decomposed exactly: the (genes x genes)
-Gram matrix of the centred ``x.T`` is formed on the device in FP64 and its top
-eigenpairs give the singular values and the cell coordinates. The reference's
+Gram matrix of the centred ``x.T`` is formed on the device in FP64, its small
+eigendecomposition runs in NumPy, and the top eigenpairs give the singular
+values and (projected on the device) the cell coordinates. The reference's
 randomized SVD approximates exactly these, so coordinates agree up to sign,
 rotation inside degenerate subspaces and the randomized solver's error.
 """
@@ -28,11 +29,12 @@ def compute_pca(m1, m2, n_components):
     n_components = min(int(n_components), x.shape[0])
     xt = x.T                                  # genes x cells
     xt = xt - xt.mean(dim=0, keepdim=True)    # PCA centring of each cell (feature)
-    gram = xt @ xt.T                          # genes x genes
-    evals, evecs = torch.linalg.eigh(gram)
-    order = torch.argsort(evals, descending=True)[:n_components]
-    s = torch.sqrt(torch.clamp(evals[order], min=0.0))
-    U = evecs[:, order]
+    gram = xt @ xt.T                          # genes x genes, FP64 GEMM on the device
+    # the eigendecomposition of this small (genes x genes) matrix runs in NumPy
+    evals, evecs = np.linalg.eigh(gram.cpu().numpy())
+    order = np.argsort(evals)[::-1][:n_components].copy()
+    s = torch.as_tensor(np.sqrt(np.clip(evals[order], 0.0, None)), device='cuda')
+    U = torch.as_tensor(evecs[:, order], device='cuda')
     comp = (xt.T @ U) / torch.where(s > 0, s, torch.ones_like(s))   # V = Xc^T U S^-1
     n1 = m1.shape[0]
     return comp[:n1], comp[n1:], s, mean_shift
