@@ -35,7 +35,8 @@ typedef enum wotg_status {
   WOTG_NONFINITE = 2,     /* reference: RuntimeError on NaN duality gap, optimal_transport.py:162-163 */
   WOTG_BADARG = 3,        /* reference: ValueError / TypeError on bad inputs */
   WOTG_CUDA_ERROR = 4,    /* a CUDA runtime call failed; see wotg_last_error() */
-  WOTG_WORKSPACE = 5      /* workspace pointer NULL or smaller than *_workspace_bytes() */
+  WOTG_WORKSPACE = 5,     /* workspace pointer NULL or smaller than *_workspace_bytes() */
+  WOTG_TOO_LARGE = 6      /* problem needs more scratch than the no-allocation entry point holds */
 } wotg_status;
 
 typedef enum wotg_solver {
@@ -130,6 +131,22 @@ int wotg_compute_transport_matrix(const wotg_problem* problem, const wotg_params
                                   double* tmap, double* learned_growth, double* row_sums,
                                   double* u_bar, double* v_bar, wotg_stats* stats,
                                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* wotg_compute_transport_matrix for callers that cannot call cudaMalloc (a host
+ * whose device memory is owned by another allocator or pool, or a path where
+ * cudaMalloc's implicit device synchronisation is not acceptable). No counterpart
+ * in the reference. Same inputs, outputs and results; the solver's scratch comes
+ * from a static 32 MiB device array (wotg_noalloc_scratch_bytes()) held by every
+ * device that loads the library until exit, instead of a caller workspace.
+ * Problems whose wotg_solve_workspace_bytes() exceeds it return WOTG_TOO_LARGE
+ * (message in wotg_last_error()). The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress); make it before any stream
+ * capture. Calls that overlap on the GPU share the array and race: serialise them.
+ * Allocates nothing. */
+size_t wotg_noalloc_scratch_bytes(void);
+int wotg_compute_transport_matrix_noalloc(const wotg_problem* problem, const wotg_params* params,
+                                          double* tmap, double* learned_growth, double* row_sums,
+                                          double* u_bar, double* v_bar, wotg_stats* stats, void* stream);
 
 /* One stabilised Sinkhorn half-step in the log domain, base 2:
  *   axis 0:  L[i] = ln2 * log2 sum_j 2^(w[j] - kappa2 C_ij)   (w: ldc floats, padding 0)

@@ -22,6 +22,7 @@ WOTG_NONFINITE = 2
 WOTG_BADARG = 3
 WOTG_CUDA_ERROR = 4
 WOTG_WORKSPACE = 5
+WOTG_TOO_LARGE = 6
 
 SOLVER_DUALITY_GAP = 0
 SOLVER_FIXED_ITERS = 1
@@ -31,7 +32,8 @@ EXPORTS = (
     'wotg_version', 'wotg_last_error', 'wotg_cost_sqeuclidean', 'wotg_cost_from_f64',
     'wotg_median_workspace_bytes', 'wotg_median', 'wotg_solve_workspace_bytes',
     'wotg_compute_transport_matrix', 'wotg_apply_coupling_f64', 'wotg_launch_count',
-    'wotg_lse_matvec_workspace_bytes', 'wotg_lse_matvec',
+    'wotg_lse_matvec_workspace_bytes', 'wotg_lse_matvec', 'wotg_noalloc_scratch_bytes',
+    'wotg_compute_transport_matrix_noalloc',
 )
 
 
@@ -84,6 +86,9 @@ def load(path: str | None = None) -> ctypes.CDLL:
                                                          vp, ctypes.c_size_t, vp]),
         'wotg_apply_coupling_f64': (ctypes.c_int, [vp, i64, i64, vp, i32, i32, i32, vp, vp]),
         'wotg_launch_count': (ctypes.c_ulonglong, []),
+        'wotg_noalloc_scratch_bytes': (ctypes.c_size_t, []),
+        'wotg_compute_transport_matrix_noalloc': (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params),
+                                                                 vp, vp, vp, vp, vp, ctypes.POINTER(Stats), vp]),
         'wotg_lse_matvec_workspace_bytes': (ctypes.c_size_t, [i64, i64, i64]),
         'wotg_lse_matvec': (ctypes.c_int, [vp, i64, i64, i64, vp, ctypes.c_float, i32, vp, vp, ctypes.c_size_t,
                                            vp]),
@@ -109,6 +114,8 @@ def check(status: int, what: str) -> int:
         raise ValueError('%s: invalid arguments' % what)
     if status == WOTG_WORKSPACE:
         raise ValueError('%s: workspace missing or too small' % what)
+    if status == WOTG_TOO_LARGE:
+        raise ValueError(load().wotg_last_error().decode())
     msg = load().wotg_last_error().decode()
     raise RuntimeError('%s: CUDA error: %s' % (what, msg))
 

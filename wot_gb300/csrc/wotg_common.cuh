@@ -17,6 +17,8 @@ constexpr float kNegBig = -1.0e30f;
 
 // Records the text of the last failing CUDA call (host side, per process).
 void set_last_error(const char* what, cudaError_t err);
+// Records a plain message as the last error text.
+void set_last_message(const char* msg);
 
 #define WOTG_CUDA(call)                                   \
   do {                                                    \

@@ -29,6 +29,8 @@ void set_last_error(const char* what, cudaError_t err) {
   snprintf(g_last_error, sizeof(g_last_error), "%s: %s", what, cudaGetErrorString(err));
 }
 
+void set_last_message(const char* msg) { snprintf(g_last_error, sizeof(g_last_error), "%s", msg); }
+
 int sm_count() {
   int dev = 0, n = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 148;

@@ -882,3 +882,62 @@ extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wot
   if (stats) *stats = total;
   return status;
 }
+
+// ---------------------------------------------------------------------------
+// No-allocation variant of wotg_compute_transport_matrix.
+//
+// Some callers cannot call cudaMalloc: hosts whose device memory is owned by
+// another allocator or pool (a JVM or Go service handing out pre-sized
+// buffers, a framework that forbids raw device allocations) and code paths
+// where cudaMalloc's implicit device synchronisation is not acceptable. They
+// still pass every input and output buffer, but get the solver's scratch from
+// the file-scope array below instead of a caller workspace.
+//
+// The array is wotg_noalloc_scratch_bytes() = 32 MiB on every device that
+// loads this module and stays allocated until the process exits. Its device
+// address is looked up once per device, on that device's first call, with
+// cudaGetSymbolAddress (host code cannot use the symbol itself: on the host it
+// names a stand-in, not device memory); make that first call before any stream
+// capture. All calls share the array: calls whose work overlaps on the GPU
+// (other streams, other host threads) race on it, so serialise them. The
+// solver re-initialises everything it reads from the scratch at the start of
+// each solve (state vectors, max slots, counters), so no clearing between
+// calls is needed.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+constexpr int kNoAllocMaxDevices = 64;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+extern "C" size_t wotg_noalloc_scratch_bytes(void) { return kNoAllocScratchBytes; }
+
+extern "C" int wotg_compute_transport_matrix_noalloc(const wotg_problem* prob, const wotg_params* params,
+                                                     double* tmap, double* learned_growth, double* row_sums,
+                                                     double* u_bar, double* v_bar, wotg_stats* stats,
+                                                     void* stream) {
+  if (!prob || !params) return WOTG_BADARG;
+  const int64_t I = prob->I, J = prob->J, ldc = prob->ldc;
+  if (I <= 0 || J <= 0 || ldc < J || (ldc & 3) || !prob->C || !prob->G) return WOTG_BADARG;
+  const size_t need = wotg_solve_workspace_bytes(I, J, ldc);
+  if (need == 0 || need > kNoAllocScratchBytes) {
+    char msg[256];
+    snprintf(msg, sizeof(msg),
+             "wotg_compute_transport_matrix_noalloc: a %lld x %lld problem needs %zu bytes of scratch, "
+             "more than the %zu-byte static array",
+             (long long)I, (long long)J, need, kNoAllocScratchBytes);
+    wotg::set_last_message(msg);
+    return WOTG_TOO_LARGE;
+  }
+  int dev = 0;
+  WOTG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return WOTG_BADARG;
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    WOTG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = p;
+  }
+  return wotg_compute_transport_matrix(prob, params, tmap, learned_growth, row_sums, u_bar, v_bar, stats,
+                                       g_noalloc_ptr[dev], kNoAllocScratchBytes, stream);
+}
