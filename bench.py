@@ -46,6 +46,8 @@ def parse():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--pair', default=None, help='I,J cells of a smaller pair (profiling runs)')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--form', default='materialized', choices=['materialized', 'onthefly', 'auto'],
+                    help='materialised FP32 cost stream or tensor-core cost recomputation')
     return ap.parse_args()
 
 
@@ -218,7 +220,7 @@ def main():
 
     def step():
         cost = D.default_cost(a, b)
-        return D.solve(cost, G, CFG, _native.SOLVER_DUALITY_GAP, want_tmap=True, tmap_out=tmap)
+        return D.solve(cost, G, CFG, _native.SOLVER_DUALITY_GAP, want_tmap=True, tmap_out=tmap, form=args.form)
 
     for _ in range(args.warmup):
         res = step()
@@ -273,8 +275,11 @@ def main():
     alg_bytes = I_FULL * J_FULL * 4 + (J_FULL + I_FULL) * 12
     peak, peak_kind = peaks()
     achieved = alg_bytes / durs[0] / 1e9
+    # DRAM bytes read + written per algorithmic byte of the row pass, from an ncu
+    # capture of the same kernel on an 8000 x 10000 pair (traffic grows with I*J)
+    traffic_ratio = (320.801280 + 3.477504) / (8000 * 10000 * 4 / 1e6)
     roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
-                'traffic': None, 'kernel': 'row_pass_kernel (wotg_lse_matvec axis 0)', 'peak_kind': peak_kind,
+                'traffic': I_FULL * J_FULL * 4 * traffic_ratio, 'kernel': 'row_pass_kernel (wotg_lse_matvec axis 0)', 'peak_kind': peak_kind,
                 'col_pass_GBps': alg_bytes / durs[1] / 1e9,
                 'row_pass_ms': durs[0] * 1e3, 'col_pass_ms': durs[1] * 1e3}
     del cost

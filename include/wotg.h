@@ -39,6 +39,11 @@ typedef enum wotg_status {
   WOTG_TOO_LARGE = 6      /* problem needs more scratch than the no-allocation entry point holds */
 } wotg_status;
 
+typedef enum wotg_form {
+  WOTG_FORM_MATERIALIZED = 0, /* stream the FP32 cost matrix every half-step (HBM-bound) */
+  WOTG_FORM_ONTHEFLY = 1      /* recompute cost tiles from the points on the tensor cores */
+} wotg_form;
+
 typedef enum wotg_solver {
   WOTG_SOLVER_DUALITY_GAP = 0, /* optimal_transport_duality_gap, optimal_transport.py:67-164 (default) */
   WOTG_SOLVER_FIXED_ITERS = 1  /* transport_stablev2, optimal_transport.py:167-236 */
@@ -82,6 +87,15 @@ typedef struct wotg_problem {
   int64_t ldc;
   double cost_scale;
   const double* G;        /* device, I (growth at the source day) */
+  /* On-the-fly form only (form == WOTG_FORM_ONTHEFLY): the FP32 points whose
+   * squared distances are C (row strides ldx, ldy floats, d <= 64). C is still
+   * required: it serves the median, sum exp(-C/eps) and the dense output. */
+  const float* X;
+  int64_t ldx;
+  const float* Y;
+  int64_t ldy;
+  int32_t d;
+  int32_t form;           /* wotg_form; 0 (materialised) when zero-initialised */
 } wotg_problem;
 
 /* Library version string and last CUDA error text (host memory, static). */
@@ -126,7 +140,8 @@ int wotg_median(const float* C, int64_t I, int64_t J, int64_t ldc, double* media
  *                   tmap = exp((u_bar_i + v_bar_j - cost_scale C_ij) / eps) / J
  *                   with eps = stats->final_epsilon.
  * stats (host) may be NULL. */
-size_t wotg_solve_workspace_bytes(int64_t I, int64_t J, int64_t ldc);
+size_t wotg_solve_workspace_bytes(int64_t I, int64_t J, int64_t ldc);   /* materialised form */
+size_t wotg_problem_workspace_bytes(const wotg_problem* problem);       /* any form */
 int wotg_compute_transport_matrix(const wotg_problem* problem, const wotg_params* params,
                                   double* tmap, double* learned_growth, double* row_sums,
                                   double* u_bar, double* v_bar, wotg_stats* stats,
@@ -157,6 +172,14 @@ int wotg_compute_transport_matrix_noalloc(const wotg_problem* problem, const wot
 size_t wotg_lse_matvec_workspace_bytes(int64_t I, int64_t J, int64_t ldc);
 int wotg_lse_matvec(const float* C, int64_t I, int64_t J, int64_t ldc, const float* w, float kappa2,
                     int32_t axis, double* L, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Diagnostics (no counterpart in the reference): one 128 x 128 x 32 tensor-core
+ * product D = A B^T through the FP16 split used by the on-the-fly form
+ * (terms = 1: hi.hi; 3: hi.hi + hi.lo + lo.hi), with the shared-memory
+ * descriptor strides given (lbo, sbo <= 512 bytes). A, B: 128 x 32 FP32
+ * row-major; D: 128 x 128 FP32; *err is set to 1 if a bounded wait timed out. */
+int wotg_tc_selftest(const float* A, const float* B, float* D, uint32_t lbo, uint32_t sbo, int32_t terms,
+                     int32_t* err, void* stream);
 
 /* Dense population transport through one FP64 coupling X (I x J, row-major):
  *   transpose == 0:  out (k x J) = P (k x I) @ X      push_forward, transport_map_model.py:290

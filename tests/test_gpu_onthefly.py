@@ -1,0 +1,90 @@
+"""The on-the-fly (tensor-core) form: the tcgen05 split-precision product,
+then whole solves against the materialised form and the oracle.
+
+Tolerances: COUPLING_TOL max|T - T_ref| / max|T_ref| <= 1e-4, as for the
+materialised form; the MMA self-test checks the FP16 hi/lo product to
+5e-6 of max|D| (hi.hi alone: 2e-3).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+COUPLING_TOL = 1e-4
+DEFAULTS = dict(growth_iters=1, epsilon=0.05, lambda1=1, lambda2=50, epsilon0=1, tau=10000, scaling_iter=3000,
+                inner_iter_max=50, tolerance=1e-8, max_iter=1e7, batch_size=5, extra_iter=1000)
+
+
+@pytest.fixture(scope='module', autouse=True)
+def built():
+    import torch
+    from wot_gb300 import _build, _native
+    assert torch.cuda.is_available()
+    _build.build()
+    _native.load()
+
+
+def err(T, R):
+    return np.abs(T - R).max() / np.abs(R).max()
+
+
+@pytest.mark.parametrize('terms,tol', [(1, 2e-3), (3, 5e-6)])
+def test_tcgen05_split_product(terms, tol):
+    import torch
+    from wot_gb300 import _native as N
+    rng = np.random.default_rng(terms)
+    A = rng.normal(size=(128, 32)).astype(np.float32)
+    B = rng.normal(size=(128, 32)).astype(np.float32)
+    At, Bt = torch.as_tensor(A, device='cuda'), torch.as_tensor(B, device='cuda')
+    D = torch.zeros((128, 128), dtype=torch.float32, device='cuda')
+    e = torch.zeros(1, dtype=torch.int32, device='cuda')
+    st = N.load().wotg_tc_selftest(At.data_ptr(), Bt.data_ptr(), D.data_ptr(), 128, 512, terms, e.data_ptr(),
+                                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    assert st == 0 and int(e.item()) == 0
+    ref = A.astype(np.float64) @ B.astype(np.float64).T
+    assert np.abs(D.cpu().numpy() - ref).max() <= tol * np.abs(ref).max()
+
+
+def _points(I, J, d, seed):
+    from wot_gb300 import synthetic
+    x = synthetic.gaussian_mixture_points(I, d=d, seed=seed)
+    y = synthetic.gaussian_mixture_points(J, d=d, seed=seed + 1)
+    g = np.random.default_rng(seed).lognormal(0, 0.3, I)
+    return x, y, g
+
+
+@pytest.mark.parametrize('I,J,d', [(37, 53, 30), (300, 257, 30), (700, 900, 30), (250, 130, 50), (129, 128, 3)])
+def test_onthefly_matches_materialized(I, J, d):
+    from wot_gb300.ot import device as D
+    x, y, g = _points(I, J, d, I + J)
+    cost = D.default_cost(x, y)
+    for solver, extra in ((0, {}), (1, dict(scaling_iter=200, extra_iter=50))):
+        cfg = dict(DEFAULTS, **extra)
+        a = D.solve(cost, g, cfg, solver, form='materialized')
+        b = D.solve(cost, g, cfg, solver, form='onthefly')
+        Ta, Tb = a.tmap.cpu().numpy(), b.tmap.cpu().numpy()
+        assert err(Tb, Ta) <= COUPLING_TOL, (solver, err(Tb, Ta))
+        if solver == 0:
+            assert abs(a.stats['iterations'] - b.stats['iterations']) <= 5
+
+
+@pytest.mark.parametrize('eps', [0.05, 0.01])
+def test_onthefly_vs_oracle_c0_shape(eps):
+    from oracle import ot_model as oom, optimal_transport as oot
+    from wot_gb300 import synthetic
+    from wot_gb300.ot import device as D
+    X, day, growth = synthetic.time_course([2000, 2500], n_genes=1000, n_clusters=6, seed=0)
+    x0, x1, s, _ = oom.compute_pca(X[day == 0], X[day == 1], 30)
+    a, b = x0 * s, x1 * s
+    C = oom.compute_default_cost_matrix(a, b)
+    G = growth[day == 0]
+    cfg = dict(DEFAULTS, epsilon=eps)
+    st = {}
+    ref = oot.optimal_transport_duality_gap(C=C, G=G, stats=st, **cfg)
+    res = D.solve(D.default_cost(a.astype(np.float32), b.astype(np.float32)), G, cfg, 0, form='onthefly')
+    T = res.tmap.cpu().numpy()
+    assert err(T, ref) <= COUPLING_TOL, err(T, ref)
+    assert abs(res.stats['iterations'] - st['iterations']) <= 10

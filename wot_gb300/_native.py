@@ -33,7 +33,7 @@ EXPORTS = (
     'wotg_median_workspace_bytes', 'wotg_median', 'wotg_solve_workspace_bytes',
     'wotg_compute_transport_matrix', 'wotg_apply_coupling_f64', 'wotg_launch_count',
     'wotg_lse_matvec_workspace_bytes', 'wotg_lse_matvec', 'wotg_noalloc_scratch_bytes',
-    'wotg_compute_transport_matrix_noalloc',
+    'wotg_compute_transport_matrix_noalloc', 'wotg_problem_workspace_bytes', 'wotg_tc_selftest',
 )
 
 
@@ -54,9 +54,15 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != 'padding_'}
 
 
+FORM_MATERIALIZED = 0
+FORM_ONTHEFLY = 1
+
+
 class Problem(ctypes.Structure):
     _fields_ = [('I', ctypes.c_int64), ('J', ctypes.c_int64), ('C', ctypes.c_void_p), ('ldc', ctypes.c_int64),
-                ('cost_scale', ctypes.c_double), ('G', ctypes.c_void_p)]
+                ('cost_scale', ctypes.c_double), ('G', ctypes.c_void_p), ('X', ctypes.c_void_p),
+                ('ldx', ctypes.c_int64), ('Y', ctypes.c_void_p), ('ldy', ctypes.c_int64), ('d', ctypes.c_int32),
+                ('form', ctypes.c_int32)]
 
 
 _lib = None
@@ -81,6 +87,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         'wotg_median_workspace_bytes': (ctypes.c_size_t, []),
         'wotg_median': (ctypes.c_int, [vp, i64, i64, i64, ctypes.POINTER(dbl), vp, ctypes.c_size_t, vp]),
         'wotg_solve_workspace_bytes': (ctypes.c_size_t, [i64, i64, i64]),
+        'wotg_problem_workspace_bytes': (ctypes.c_size_t, [ctypes.POINTER(Problem)]),
+        'wotg_tc_selftest': (ctypes.c_int, [vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, i32, vp, vp]),
         'wotg_compute_transport_matrix': (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params),
                                                          vp, vp, vp, vp, vp, ctypes.POINTER(Stats),
                                                          vp, ctypes.c_size_t, vp]),

@@ -32,6 +32,7 @@
 #include <cstring>
 
 #include "wotg_common.cuh"
+#include "wotg_onthefly.cuh"
 
 namespace wotg {
 
@@ -65,7 +66,25 @@ struct Coef {
   double inv_l1e, inv_l2e;  // 1/(lambda + eps)
   double lambda1, lambda2;
   double logI, logJ, logq, q;
+  double kappa;             // cost_scale / eps
   float kappa2;             // cost_scale / eps * log2(e)
+};
+
+// Buffers of the on-the-fly (tensor-core) form.
+struct TcState {
+  bool on;
+  int kp;                   // packed dimension (32 or 64)
+  int n_xt, n_yt;           // 128-point tiles of X and Y
+  int64_t I_pad, J_pad;
+  int nsplit_row, nsplit_col;
+  __half* Xt;
+  __half* Yt;
+  double* normX;            // |x_i|^2 (FP64)
+  double* normY;
+  float* bias_row;          // J_pad: bias over columns for the row pass
+  float* bias_col;          // I_pad: bias over rows for the column pass
+  float2* part;
+  int* err;
 };
 
 struct Geom {
@@ -470,6 +489,43 @@ __global__ void __launch_bounds__(256) coupling_kernel(const float* __restrict__
 }
 
 // ---------------------------------------------------------------------------
+// On-the-fly form: per-half-step biases and the FP64 merge of the tensor-core
+// kernel's partials. The exponent of element (i, j) is split as
+//   bias_j + gamma (x_i . y_j) - kappa2 |x_i|^2,   gamma = 2 kappa2,
+//   bias_j = (v_j / eps + lb_j) log2 e - kappa2 |y_j|^2     (FP64, rounded once),
+// i.e. (v_j/eps + lb_j - kappa C_ij) in base 2 with C = |x|^2 + |y|^2 - 2 x.y.
+// ---------------------------------------------------------------------------
+__global__ void tc_bias_kernel(int64_t n, int64_t n_pad, const double* __restrict__ pot,
+                               const double* __restrict__ lsc, const double* __restrict__ norm, double inv_eps,
+                               double kappa2d, float* __restrict__ bias) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += (int64_t)gridDim.x * blockDim.x)
+    bias[i] = i < n ? (float)((pot[i] * inv_eps + lsc[i]) * kLog2e - kappa2d * norm[i]) : -INFINITY;
+}
+
+template <bool ROW, bool UPDATE>
+__global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restrict__ part, int nsplit,
+                                  int64_t n_pad, const double* __restrict__ norm, int parity) {
+  const int64_t n = ROW ? g.I : g.J;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float mx = kNegBig;
+  for (int r = 0; r < nsplit; ++r) mx = fmaxf(mx, part[(int64_t)r * n_pad + i].x);
+  double s = 0.0;
+  for (int r = 0; r < nsplit; ++r) {
+    const float2 ps = part[(int64_t)r * n_pad + i];
+    s += (double)ps.y * (double)ex2(ps.x - mx);
+  }
+  const double L = ((double)mx + log2(s)) * kLn2 - c.kappa * norm[i];
+  if (ROW) {
+    V.Lrow[i] = L;
+    if (UPDATE) a_update(i, L, V, c, V.maxslot + parity);
+  } else {
+    V.Lcol[i] = L;
+    if (UPDATE) b_update(i, L, V, c, V.maxslot + parity);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 struct Solver {
@@ -479,6 +535,7 @@ struct Solver {
   cudaStream_t st;
   double cost_scale;
   int small_grid;  // grid for O(I+J) kernels
+  TcState tc;
 
   Coef coef(double eps, const wotg_params& P, double q) const {
     Coef c;
@@ -494,14 +551,53 @@ struct Solver {
     c.logJ = std::log((double)g.J);
     c.q = q;
     c.logq = std::log(q);
+    c.kappa = cost_scale / eps;
     c.kappa2 = (float)(cost_scale / eps * kLog2e);
     return c;
   }
 
   int vec_blocks(int64_t n) const { return (int)std::max<int64_t>(1, (n + 255) / 256); }
 
+  // On-the-fly row pass (K (b dy)) / column pass (K^T (a dx)).
+  template <bool UPDATE>
+  int tc_row_pass(const Coef& c, int parity) {
+    tc_bias_kernel<<<vec_blocks(tc.J_pad), 256, 0, st>>>(g.J, tc.J_pad, V.v, V.lb, tc.normY, c.inv_eps,
+                                                         c.kappa * kLog2e, tc.bias_row);
+    WOTG_LAUNCHED();
+    int s = tc_lse_launch(tc.Xt, tc.n_xt, tc.Yt, tc.n_yt, tc.bias_row, tc.kp, 2.0f * c.kappa2, tc.nsplit_row,
+                          tc.part, tc.I_pad, tc.err, st);
+    if (s) return s;
+    tc_combine_kernel<true, UPDATE><<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, tc.part, tc.nsplit_row, tc.I_pad,
+                                                                     tc.normX, parity);
+    WOTG_LAUNCHED();
+    return WOTG_OK;
+  }
+  int tc_col_pass(const Coef& c, int parity) {
+    tc_bias_kernel<<<vec_blocks(tc.I_pad), 256, 0, st>>>(g.I, tc.I_pad, V.u, V.la, tc.normX, c.inv_eps,
+                                                         c.kappa * kLog2e, tc.bias_col);
+    WOTG_LAUNCHED();
+    int s = tc_lse_launch(tc.Yt, tc.n_yt, tc.Xt, tc.n_xt, tc.bias_col, tc.kp, 2.0f * c.kappa2, tc.nsplit_col,
+                          tc.part, tc.J_pad, tc.err, st);
+    if (s) return s;
+    tc_combine_kernel<false, true><<<vec_blocks(g.J), 256, 0, st>>>(g, V, c, tc.part, tc.nsplit_col, tc.J_pad,
+                                                                    tc.normY, parity);
+    WOTG_LAUNCHED();
+    return WOTG_OK;
+  }
+
   int iteration(const Coef& c, bool lrow_valid, int parity, bool update_b_only = false) {
     (void)update_b_only;
+    if (tc.on) {
+      int s;
+      if (lrow_valid) {
+        a_update_kernel<<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, parity);
+        WOTG_LAUNCHED();
+      } else {
+        s = tc_row_pass<true>(c, parity);
+        if (s) return s;
+      }
+      return tc_col_pass(c, parity);
+    }
     if (lrow_valid) {
       a_update_kernel<<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, parity);
     } else {
@@ -556,6 +652,7 @@ struct Solver {
   }
 
   int fresh_lrow(const Coef& c) {
+    if (tc.on) return tc_row_pass<false>(c, 0);
     row_pass_kernel<false><<<g.row_grid, 256, 0, st>>>(C, g, V, c, 0);
     WOTG_LAUNCHED();
     return WOTG_OK;
@@ -797,6 +894,70 @@ extern "C" int wotg_lse_matvec(const float* C, int64_t I, int64_t J, int64_t ldc
   return WOTG_OK;
 }
 
+// Split of the other set's tiles across CTAs that fills whole waves of the
+// tensor-core kernel as well as possible (ties: more CTAs).
+static int pick_nsplit(int row_tiles, int col_tiles, int slots) {
+  int best = 1;
+  double best_eff = -1.0;
+  const int cap = std::max(1, std::min(col_tiles, 64));
+  for (int ns = 1; ns <= cap; ++ns) {
+    const double ctas = (double)row_tiles * ns;
+    const double waves = std::ceil(ctas / slots);
+    double eff = ctas / (waves * slots);
+    if (ctas < slots) eff *= 0.5 + 0.5 * ctas / slots;
+    if (eff > best_eff + 1e-9 || (std::fabs(eff - best_eff) <= 1e-9 && ns > best)) {
+      best = ns;
+      best_eff = eff;
+    }
+  }
+  return best;
+}
+
+static bool tc_requested(const wotg_problem* prob) { return prob->form == WOTG_FORM_ONTHEFLY; }
+
+static int tc_valid(const wotg_problem* prob) {
+  if (!tc_requested(prob)) return prob->form == WOTG_FORM_MATERIALIZED ? WOTG_OK : WOTG_BADARG;
+  if (!prob->X || !prob->Y || prob->d < 1 || prob->d > 64 || prob->ldx < prob->d || prob->ldy < prob->d)
+    return WOTG_BADARG;
+  return WOTG_OK;
+}
+
+static void tc_layout(Bump& b, const wotg_problem* prob, TcState& tc) {
+  tc.on = true;
+  tc.kp = tc_kp(prob->d);
+  tc.n_xt = (int)((prob->I + 127) / 128);
+  tc.n_yt = (int)((prob->J + 127) / 128);
+  tc.I_pad = (int64_t)tc.n_xt * 128;
+  tc.J_pad = (int64_t)tc.n_yt * 128;
+  const int slots = sm_count() * std::max(1, tc_ctas_per_sm(tc.kp));
+  tc.nsplit_row = pick_nsplit(tc.n_xt, tc.n_yt, slots);
+  tc.nsplit_col = pick_nsplit(tc.n_yt, tc.n_xt, slots);
+  const size_t tb = tc_tile_bytes(tc.kp);
+  tc.Xt = reinterpret_cast<__half*>(b.take<unsigned char>(tb * tc.n_xt));
+  tc.Yt = reinterpret_cast<__half*>(b.take<unsigned char>(tb * tc.n_yt));
+  tc.normX = b.take<double>(prob->I);
+  tc.normY = b.take<double>(prob->J);
+  tc.bias_row = b.take<float>(tc.J_pad);
+  tc.bias_col = b.take<float>(tc.I_pad);
+  tc.part = b.take<float2>(std::max((size_t)tc.nsplit_row * tc.I_pad, (size_t)tc.nsplit_col * tc.J_pad));
+  tc.err = b.take<int>(4);
+}
+
+extern "C" size_t wotg_problem_workspace_bytes(const wotg_problem* prob) {
+  if (!prob || prob->I <= 0 || prob->J <= 0 || prob->ldc < prob->J || tc_valid(prob) != WOTG_OK) return 0;
+  Geom g = make_geom(prob->I, prob->J, prob->ldc);
+  Bump b{nullptr, 0};
+  Vecs V{};
+  b.take<double>(prob->I);
+  size_t n = layout(b, g, V);
+  if (tc_requested(prob)) {
+    TcState tc{};
+    tc_layout(b, prob, tc);
+    n = b.off + 256;
+  }
+  return n;
+}
+
 extern "C" size_t wotg_solve_workspace_bytes(int64_t I, int64_t J, int64_t ldc) {
   if (I <= 0 || J <= 0 || ldc < J) return 0;
   Geom g = make_geom(I, J, ldc);
@@ -824,7 +985,8 @@ extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wot
   } else {
     return WOTG_BADARG;
   }
-  if (!workspace || workspace_bytes < wotg_solve_workspace_bytes(I, J, ldc)) return WOTG_WORKSPACE;
+  if (tc_valid(prob) != WOTG_OK) return WOTG_BADARG;
+  if (!workspace || workspace_bytes < wotg_problem_workspace_bytes(prob)) return WOTG_WORKSPACE;
 
   Geom g = make_geom(I, J, ldc);
   // layout() leaves 256 bytes of slack for aligning the caller's base pointer
@@ -833,7 +995,15 @@ extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wot
   Vecs V{};
   layout(b, g, V);
   cudaStream_t st = (cudaStream_t)stream;
-  Solver S{prob->C, g, V, st, prob->cost_scale, 0};
+  Solver S{prob->C, g, V, st, prob->cost_scale, 0, TcState{}};
+  if (tc_requested(prob)) {
+    tc_layout(b, prob, S.tc);
+    WOTG_CUDA(cudaMemsetAsync(S.tc.err, 0, sizeof(int), st));
+    int s = tc_pack_points(prob->X, I, prob->ldx, prob->d, S.tc.kp, S.tc.Xt, S.tc.normX, st);
+    if (s) return s;
+    s = tc_pack_points(prob->Y, J, prob->ldy, prob->d, S.tc.kp, S.tc.Yt, S.tc.normY, st);
+    if (s) return s;
+  }
 
   wotg_stats total{};
   int status = WOTG_OK;
@@ -879,6 +1049,14 @@ extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wot
     }
   }
   WOTG_CUDA(cudaStreamSynchronize(st));
+  if (S.tc.on) {
+    int err = 0;
+    WOTG_CUDA(cudaMemcpy(&err, S.tc.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+      set_last_message("tensor-core half-step: a bounded wait timed out");
+      return WOTG_CUDA_ERROR;
+    }
+  }
   if (stats) *stats = total;
   return status;
 }
@@ -920,7 +1098,7 @@ extern "C" int wotg_compute_transport_matrix_noalloc(const wotg_problem* prob, c
   if (!prob || !params) return WOTG_BADARG;
   const int64_t I = prob->I, J = prob->J, ldc = prob->ldc;
   if (I <= 0 || J <= 0 || ldc < J || (ldc & 3) || !prob->C || !prob->G) return WOTG_BADARG;
-  const size_t need = wotg_solve_workspace_bytes(I, J, ldc);
+  const size_t need = wotg_problem_workspace_bytes(prob);
   if (need == 0 || need > kNoAllocScratchBytes) {
     char msg[256];
     snprintf(msg, sizeof(msg),

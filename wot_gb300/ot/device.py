@@ -23,12 +23,17 @@ DEFAULTS = {'growth_iters': 1, 'epsilon': 0.05, 'lambda1': 1, 'lambda2': 50, 'ep
 
 @dataclass
 class DeviceCost:
-    """FP32 cost on the device, I x ldc with +inf padding; reference cost = scale * C."""
+    """FP32 cost on the device, I x ldc with +inf padding; reference cost = scale * C.
+
+    When built from points, ``X`` / ``Y`` keep the FP32 points so that the
+    on-the-fly (tensor-core) form can recompute cost tiles."""
     C: object
     I: int
     J: int
     ldc: int
     scale: float = 1.0
+    X: object = None
+    Y: object = None
 
     @property
     def shape(self):
@@ -94,7 +99,7 @@ def cost_from_points(x, y) -> DeviceCost:
     C32 = torch.empty((I, ldc), dtype=torch.float32, device='cuda')
     N.check(N.load().wotg_cost_sqeuclidean(X.data_ptr(), I, X.stride(0), Y.data_ptr(), J, Y.stride(0), d,
                                            C32.data_ptr(), ldc, _stream()), 'wotg_cost_sqeuclidean')
-    return DeviceCost(C32, I, J, ldc, 1.0)
+    return DeviceCost(C32, I, J, ldc, 1.0, X, Y)
 
 
 def median(cost: DeviceCost) -> float:
@@ -129,8 +134,24 @@ def make_params(cfg: dict, solver: int) -> N.Params:
                     extra_iter=int(p['extra_iter']), growth_iters=int(p['growth_iters']), solver=int(solver))
 
 
+FORMS = {'materialized': N.FORM_MATERIALIZED, 'onthefly': N.FORM_ONTHEFLY}
+
+
+def resolve_form(cost: DeviceCost, form: str) -> int:
+    """'materialized' streams the FP32 cost; 'onthefly' recomputes cost tiles
+    from the points on the tensor cores; 'auto' picks the latter when the cost
+    was built from points of at most 64 dimensions."""
+    if form == 'auto':
+        form = 'onthefly' if cost.X is not None and cost.X.shape[1] <= 64 else 'materialized'
+    if form not in FORMS:
+        raise ValueError("form must be 'auto', 'materialized' or 'onthefly'")
+    if form == 'onthefly' and cost.X is None:
+        raise ValueError('the on-the-fly form needs a cost built from points')
+    return FORMS[form]
+
+
 def solve(cost: DeviceCost, G, cfg: dict, solver: int = N.SOLVER_DUALITY_GAP, want_tmap: bool = True,
-          want_potentials: bool = False, tmap_out=None) -> SolveResult:
+          want_potentials: bool = False, tmap_out=None, form: str = 'materialized') -> SolveResult:
     """All growth iterations of one transport problem on the device
     (wot.ot.compute_transport_matrix, optimal_transport.py:10-33)."""
     torch = _torch()
@@ -148,10 +169,16 @@ def solve(cost: DeviceCost, G, cfg: dict, solver: int = N.SOLVER_DUALITY_GAP, wa
         tmap = tmap_out if tmap_out is not None else torch.empty((I, J), dtype=torch.float64, device='cuda')
     u_bar = torch.empty(I, dtype=torch.float64, device='cuda') if want_potentials else None
     v_bar = torch.empty(J, dtype=torch.float64, device='cuda') if want_potentials else None
-    nbytes = lib.wotg_solve_workspace_bytes(I, J, cost.ldc)
-    ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
     prob = N.Problem(I=I, J=J, C=cost.C.data_ptr(), ldc=cost.ldc, cost_scale=float(cost.scale),
                      G=Gd.data_ptr())
+    if resolve_form(cost, form) == N.FORM_ONTHEFLY:
+        prob.X, prob.ldx = cost.X.data_ptr(), cost.X.stride(0)
+        prob.Y, prob.ldy = cost.Y.data_ptr(), cost.Y.stride(0)
+        prob.d, prob.form = cost.X.shape[1], N.FORM_ONTHEFLY
+    nbytes = lib.wotg_problem_workspace_bytes(ctypes.byref(prob))
+    if nbytes == 0:
+        raise ValueError('invalid transport problem')
+    ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
     stats = N.Stats()
     status = lib.wotg_compute_transport_matrix(ctypes.byref(prob), ctypes.byref(params), N.ptr(tmap),
                                                learned.data_ptr(), row_sums.data_ptr(), N.ptr(u_bar),
