@@ -123,62 +123,149 @@ __global__ void tc_pack_kernel(const float* __restrict__ X, int64_t n, int64_t l
 }
 
 // ---------------------------------------------------------------------------
-// On-the-fly half-step: for each point p_i of a 128-point row tile and the
-// column tiles [q0, q1) of the other set, the base-2 log-sum-exp partial
-//   (m_i, s_i):  s_i 2^m_i = sum_j 2^(bias_j + gamma (p_i . q_j))
-// where p . q comes from the FP16 split-precision MMA (hi.hi + hi.lo + lo.hi,
-// FP32 accumulation in TMEM). The row term of the exponent (-kappa |p_i|^2)
-// and the FP64 merge of the partials are applied by the caller.
+// On-the-fly half-step: base-2 log-sum-exp partials
+//   (m, s):  s 2^m = sum_j 2^(bias_j + gamma (p_i . q_j))
+// over 128-point tiles of the other set, where p . q comes from the FP16
+// split-precision MMA (hi.hi + hi.lo + lo.hi, FP32 accumulation in TMEM). The
+// row term of the exponent (-kappa |p_i|^2) and the FP64 merge of the partials
+// are applied by the caller.
 //
-// CTA: 256 threads = 2 warpgroups; TMEM accumulator 128 lanes x 128 columns;
-// warpgroup g reads columns [64 g, 64 g + 64) of every row. The A tile is loaded
-// once; B tiles and their 128 biases are double-buffered through bulk
-// asynchronous copies so that the copy of tile k+1 overlaps tile k. Every wait
-// is bounded: on a timeout the CTA sets *err, stops, waits (bounded) for what it
-// issued and frees its TMEM.
+// Persistent schedule: the n_pt x nq (row tile, column tile) pairs are walked
+// row-major and cut into gridDim.x contiguous, equal stretches, one per CTA. A
+// stretch covers one or more row tiles ("segments"); at the end of each
+// segment the CTA writes, for every row of that row tile and each of the four
+// 32-column quarters, one partial at part[((cta + tile) * 128 + row) * 4 + quarter].
+// Along the walk (cta, tile) only ever steps up, so cta + tile indexes every
+// (CTA, row tile) segment uniquely.
+//
+// Warp roles (18 warps, one CTA per SM):
+//   warp 0      producer: bulk asynchronous copies of A tiles (one per segment,
+//               two buffers) and B tiles (a kStages-deep ring);
+//   warp 1      MMA issuer: 6 split-precision MMAs per tile into one of four
+//               128 x 128 FP32 TMEM accumulators; owns the TMEM allocation;
+//   warps 2-17  epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 and the
+//               32 columns of quarter (w - 2) / 4, adds the column biases (read
+//               through L1) and folds them into a running (max, sum).
+// mbarriers hand buffers between roles (full / empty per B stage, per A buffer
+// and per accumulator). Every wait is bounded: a role that times out sets *err
+// and stops; the others then time out in turn, and TMEM is freed at the end.
 // ---------------------------------------------------------------------------
+constexpr int kTcStages = 6;
+constexpr int kTcAcc = 4;            // TMEM accumulators (128 columns each)
+constexpr int kTcEpiWarps = 16;
+constexpr int kTcThreads = 32 * (2 + kTcEpiWarps);
+
 template <int KP>
 struct TcSmem {
   static constexpr uint32_t kHalfBytes = 128u * KP * 2u;      // one of hi / lo
-  static constexpr uint32_t kTileBytes = 2u * kHalfBytes;      // hi + lo
-  static constexpr uint32_t kA = 0;
-  static constexpr uint32_t kB = kTileBytes;                   // 2 buffers
-  static constexpr uint32_t kBias = kB + 2 * kTileBytes;       // 2 x 128 floats
-  static constexpr uint32_t kBar = kBias + 2 * 512;            // 3 mbarriers + TMEM slot
-  static constexpr uint32_t kMerge = kBar + 64;                // 128 float2
-  static constexpr uint32_t kBytes = kMerge + 128 * 8;
+  static constexpr uint32_t kTileBytes = 2u * kHalfBytes;      // packed 128-point tile (hi + lo)
+  static constexpr int kStages = KP == 32 ? kTcStages : 2;     // B ring depth (shared-memory budget)
+  static constexpr uint32_t kA = 0;                            // 2 buffers
+  static constexpr uint32_t kB = 2 * kTileBytes;               // kStages buffers
+  static constexpr uint32_t kBar = kB + kStages * kTileBytes;
+  // barriers: full[S], empty[S], a_full[2], a_empty[2], acc_full[4], acc_empty[4], TMEM slot
+  static constexpr uint32_t kBytes = kBar + 8 * (2 * kStages + 4 + 2 * kTcAcc) + 16;
   static constexpr uint32_t kAlloc = kBytes + 1024;            // slack for 1024-byte alignment
+  static constexpr uint32_t kTmemCols = 128 * kTcAcc;
 };
 
 template <int KP>
-__global__ void __launch_bounds__(256, 3) lse_tc_kernel(const __half* __restrict__ Pt, const __half* __restrict__ Qt,
-                                                        const float* __restrict__ bias, int nqt, int nsplit,
-                                                        float gamma, float2* __restrict__ part, int64_t n_pad,
-                                                        int* __restrict__ err) {
+__device__ __forceinline__ void tc_issue_mma(uint32_t tmem_d, uint32_t sAt, uint32_t sBt) {
   using L = TcSmem<KP>;
+  constexpr uint32_t idesc = tc::idesc_f16_f32(128, 128);
+  constexpr uint32_t sbo = KP * 16;
+#pragma unroll
+  for (int st = 0; st < KP / 16; ++st) {
+    const uint32_t ko = (uint32_t)st * 2u * tc::kCoreLbo;
+    const uint64_t ahi = tc::smem_desc(sAt + ko, tc::kCoreLbo, sbo);
+    const uint64_t alo = tc::smem_desc(sAt + L::kHalfBytes + ko, tc::kCoreLbo, sbo);
+    const uint64_t bhi = tc::smem_desc(sBt + ko, tc::kCoreLbo, sbo);
+    const uint64_t blo = tc::smem_desc(sBt + L::kHalfBytes + ko, tc::kCoreLbo, sbo);
+    tc::mma_f16(tmem_d, ahi, bhi, idesc, st > 0 ? 1u : 0u);
+    tc::mma_f16(tmem_d, ahi, blo, idesc, 1u);
+    tc::mma_f16(tmem_d, alo, bhi, idesc, 1u);
+  }
+}
+
+// Online LSE of 32 exponents gamma * d[c] + b[c] into (m, s): packed FP32x2
+// arithmetic and tree reductions.
+__device__ __forceinline__ void lse32(const float (&d)[32], const float4* __restrict__ b4, float gamma, float& m,
+                                      float& s) {
+  float2 x[16];
+  const float2 g2 = make_float2(gamma, gamma);
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const float4 b = __ldg(b4 + c);
+    x[2 * c] = __ffma2_rn(g2, make_float2(d[4 * c], d[4 * c + 1]), make_float2(b.x, b.y));
+    x[2 * c + 1] = __ffma2_rn(g2, make_float2(d[4 * c + 2], d[4 * c + 3]), make_float2(b.z, b.w));
+  }
+  float mx[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) mx[c] = fmaxf(fmaxf(x[2 * c].x, x[2 * c].y), fmaxf(x[2 * c + 1].x, x[2 * c + 1].y));
+#pragma unroll
+  for (int w = 4; w >= 1; w >>= 1)
+#pragma unroll
+    for (int c = 0; c < w; ++c) mx[c] = fmaxf(mx[c], mx[c + w]);
+  const float mn = fmaxf(m, mx[0]);
+  const float2 neg = make_float2(-mn, -mn);
+  float2 e[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    const float2 z = __fadd2_rn(x[c], neg);
+    e[c] = make_float2(ex2(z.x), ex2(z.y));
+  }
+#pragma unroll
+  for (int w = 8; w >= 1; w >>= 1)
+#pragma unroll
+    for (int c = 0; c < w; ++c) e[c] = __fadd2_rn(e[c], e[c + w]);
+  s = s * ex2(m - mn) + (e[0].x + e[0].y);
+  m = mn;
+}
+
+template <int KP>
+__global__ void __launch_bounds__(kTcThreads, 1) lse_tc_kernel(const __half* __restrict__ Pt,
+                                                               const __half* __restrict__ Qt,
+                                                               const float* __restrict__ bias, int n_pt, int nq,
+                                                               float gamma, float2* __restrict__ part,
+                                                               int* __restrict__ err) {
+  using L = TcSmem<KP>;
+  constexpr int S = L::kStages;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                          ~uintptr_t(1023));
-  uint64_t* bar_ld = reinterpret_cast<uint64_t*>(smem + L::kBar);  // [2]
-  uint64_t* bar_mma = bar_ld + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_ld + 3);
-  float2* merge = reinterpret_cast<float2*>(smem + L::kMerge);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::kBar);
+  uint64_t* empty = full + S;
+  uint64_t* a_full = empty + S;
+  uint64_t* a_empty = a_full + 2;
+  uint64_t* acc_full = a_empty + 2;
+  uint64_t* acc_empty = acc_full + kTcAcc;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + kTcAcc);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int wg = warp >> 2, wq = warp & 3;
-  const int t = blockIdx.y, sp = blockIdx.x;
-  const int q0 = (int)((int64_t)sp * nqt / nsplit);
-  const int q1 = (int)((int64_t)(sp + 1) * nqt / nsplit);
-  const int ntiles = q1 - q0;
+  const int64_t total = (int64_t)n_pt * nq;
+  const int64_t f0 = tc_stretch_begin(blockIdx.x, total, gridDim.x);
+  const int64_t f1 = tc_stretch_begin(blockIdx.x + 1, total, gridDim.x);
+  const int n = (int)(f1 - f0);
   const int64_t tile_halfs = (int64_t)2 * 128 * KP;
+  const int t_first = (int)(f0 / nq);
+  const int q_first = (int)(f0 % nq);
 
-  if (warp == 0) {
-    tc::tmem_alloc(tmem_slot, 128);
+  if (warp == 1) {
+    tc::tmem_alloc(tmem_slot, L::kTmemCols);
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    tc::mbar_init(&bar_ld[0], 1);
-    tc::mbar_init(&bar_ld[1], 1);
-    tc::mbar_init(bar_mma, 1);
+    for (int b = 0; b < S; ++b) {
+      tc::mbar_init(&full[b], 1);
+      tc::mbar_init(&empty[b], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&a_full[b], 1);
+      tc::mbar_init(&a_empty[b], 1);
+    }
+    for (int b = 0; b < kTcAcc; ++b) {
+      tc::mbar_init(&acc_full[b], 1);
+      tc::mbar_init(&acc_empty[b], kTcEpiWarps);
+    }
     tc::mbar_fence_init();
   }
   tc::fence_before_sync();
@@ -187,93 +274,98 @@ __global__ void __launch_bounds__(256, 3) lse_tc_kernel(const __half* __restrict
   const uint32_t tmem = *tmem_slot;
   const uint32_t sA = tc::smem_u32(smem + L::kA);
   const uint32_t sB = tc::smem_u32(smem + L::kB);
-  const uint32_t sBias = tc::smem_u32(smem + L::kBias);
-  if (tid == 0 && ntiles > 0) {
-    tc::mbar_expect_tx(&bar_ld[0], 2 * L::kTileBytes + 512);
-    tc::bulk_g2s(sA, Pt + (int64_t)t * tile_halfs, L::kTileBytes, &bar_ld[0]);
-    tc::bulk_g2s(sB, Qt + (int64_t)q0 * tile_halfs, L::kTileBytes, &bar_ld[0]);
-    tc::bulk_g2s(sBias, bias + (int64_t)q0 * 128, 512, &bar_ld[0]);
-  }
-  constexpr uint32_t idesc = tc::idesc_f16_f32(128, 128);
-  constexpr uint32_t sbo = KP * 16;
-  float m = kNegBig, s = 0.f;
-  bool ok = true;
-  bool next_issued = false;
-  int k = 0;
-  for (; k < ntiles; ++k) {
-    const int buf = k & 1;
-    bool good = tc::mbar_wait(&bar_ld[buf], (uint32_t)((k >> 1) & 1), kTcWaitTries);
-    next_issued = false;
-    if (tid == 0) {
-      if (k + 1 < ntiles) {
-        const uint32_t nb = (uint32_t)(buf ^ 1);
-        tc::mbar_expect_tx(&bar_ld[nb], L::kTileBytes + 512);
-        tc::bulk_g2s(sB + nb * L::kTileBytes, Qt + (int64_t)(q0 + k + 1) * tile_halfs, L::kTileBytes, &bar_ld[nb]);
-        tc::bulk_g2s(sBias + nb * 512, bias + (int64_t)(q0 + k + 1) * 128, 512, &bar_ld[nb]);
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer
+      int t = t_first, q = q_first, seg = 0;
+      for (int j = 0; j < n; ++j) {
+        const int stage = j % S;
+        if (j >= S && !tc::mbar_wait(&empty[stage], (uint32_t)((j / S - 1) & 1), kTcWaitTries)) {
+          atomicExch(err, 1);
+          break;
+        }
+        if (j == 0 || q == 0) {
+          if (j > 0) ++seg;
+          if (seg >= 2 && !tc::mbar_wait(&a_empty[seg & 1], (uint32_t)(((seg >> 1) - 1) & 1), kTcWaitTries)) {
+            atomicExch(err, 1);
+            break;
+          }
+          tc::mbar_expect_tx(&a_full[seg & 1], L::kTileBytes);
+          tc::bulk_g2s(sA + (uint32_t)(seg & 1) * L::kTileBytes, Pt + (int64_t)t * tile_halfs, L::kTileBytes,
+                       &a_full[seg & 1]);
+        }
+        tc::mbar_expect_tx(&full[stage], L::kTileBytes);
+        tc::bulk_g2s(sB + (uint32_t)stage * L::kTileBytes, Qt + (int64_t)q * tile_halfs, L::kTileBytes,
+                     &full[stage]);
+        if (++q == nq) {
+          q = 0;
+          ++t;
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer
+      int q = q_first, seg = 0;
+      for (int j = 0; j < n; ++j) {
+        const int stage = j % S, b = j % kTcAcc;
+        const bool new_seg = j == 0 || q == 0;
+        if (new_seg && j > 0) ++seg;
+        bool good = true;
+        if (new_seg) good = tc::mbar_wait(&a_full[seg & 1], (uint32_t)((seg >> 1) & 1), kTcWaitTries);
+        good = good && tc::mbar_wait(&full[stage], (uint32_t)((j / S) & 1), kTcWaitTries);
+        if (j >= kTcAcc)
+          good = good && tc::mbar_wait(&acc_empty[b], (uint32_t)((j / kTcAcc - 1) & 1), kTcWaitTries);
+        if (!good) {
+          atomicExch(err, 1);
+          break;
+        }
+        tc::fence_after_sync();
+        tc_issue_mma<KP>(tmem + (uint32_t)(128 * b), sA + (uint32_t)(seg & 1) * L::kTileBytes,
+                         sB + (uint32_t)stage * L::kTileBytes);
+        tc::mma_commit(&empty[stage]);
+        tc::mma_commit(&acc_full[b]);
+        if (++q == nq) q = 0;
+        if (j == n - 1 || q == 0) tc::mma_commit(&a_empty[seg & 1]);
+      }
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, columns of quarter (w - 2) / 4
+    const int wq = warp & 3, cq = (warp - 2) >> 2;
+    const int row = 32 * wq + lane;
+    float m = kNegBig, s = 0.f;
+    int t = t_first, q = q_first;
+    for (int j = 0; j < n; ++j) {
+      const int b = j % kTcAcc;
+      const bool good =
+          __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[b], (uint32_t)((j / kTcAcc) & 1), kTcWaitTries));
+      if (!good) {
+        if (lane == 0) atomicExch(err, 1);
+        break;
       }
       tc::fence_after_sync();
-      const uint32_t b0 = sB + (uint32_t)buf * L::kTileBytes;
-#pragma unroll
-      for (int st = 0; st < KP / 16; ++st) {
-        const uint32_t ko = (uint32_t)st * 2u * tc::kCoreLbo;
-        const uint64_t ahi = tc::smem_desc(sA + ko, tc::kCoreLbo, sbo);
-        const uint64_t alo = tc::smem_desc(sA + L::kHalfBytes + ko, tc::kCoreLbo, sbo);
-        const uint64_t bhi = tc::smem_desc(b0 + ko, tc::kCoreLbo, sbo);
-        const uint64_t blo = tc::smem_desc(b0 + L::kHalfBytes + ko, tc::kCoreLbo, sbo);
-        tc::mma_f16(tmem, ahi, bhi, idesc, st > 0 ? 1u : 0u);
-        tc::mma_f16(tmem, ahi, blo, idesc, 1u);
-        tc::mma_f16(tmem, alo, bhi, idesc, 1u);
-      }
-      tc::mma_commit(bar_mma);
-    }
-    next_issued = k + 1 < ntiles;
-    good = tc::mbar_wait(bar_mma, (uint32_t)(k & 1), kTcWaitTries) && good;
-    good = __all_sync(0xffffffffu, good);
-    tc::fence_after_sync();
-    if (good) {
-      const float* bt = reinterpret_cast<const float*>(smem + L::kBias + buf * 512) + 64 * wg;
-#pragma unroll 1
-      for (int h = 0; h < 2; ++h) {
-        float v[32];
-        tc::tmem_ld32(tmem + ((uint32_t)(32 * wq) << 16) + (uint32_t)(64 * wg + 32 * h), v);
-        tc::tmem_wait_ld();
-        float mx = kNegBig;
-#pragma unroll
-        for (int c = 0; c < 32; ++c) {
-          v[c] = fmaf(gamma, v[c], bt[32 * h + c]);
-          mx = fmaxf(mx, v[c]);
+      float d[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(32 * wq) << 16) + (uint32_t)(128 * b + 32 * cq), d);
+      tc::tmem_wait_ld();
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+      lse32(d, reinterpret_cast<const float4*>(bias + (int64_t)q * 128 + 32 * cq), gamma, m, s);
+      if (++q == nq || j == n - 1) {
+        part[(((int64_t)blockIdx.x + t) * 128 + row) * 4 + cq] = make_float2(m, s);
+        m = kNegBig;
+        s = 0.f;
+        if (q == nq) {
+          q = 0;
+          ++t;
         }
-        const float mn = fmaxf(m, mx);
-        float acc = 0.f;
-#pragma unroll
-        for (int c = 0; c < 32; ++c) acc += ex2(v[c] - mn);
-        s = s * ex2(m - mn) + acc;
-        m = mn;
       }
-    }
-    tc::fence_before_sync();
-    ok = __syncthreads_and(good) != 0;
-    if (!ok) break;
-  }
-  if (!ok) {
-    if (tid == 0) atomicExch(err, 1);
-    // bounded waits for the copies / MMAs this CTA issued, then release TMEM
-    tc::mbar_wait(&bar_ld[k & 1], (uint32_t)((k >> 1) & 1), kTcWaitTries);
-    if (next_issued) tc::mbar_wait(&bar_ld[(k & 1) ^ 1], (uint32_t)(((k + 1) >> 1) & 1), kTcWaitTries);
-    tc::mbar_wait(bar_mma, (uint32_t)(k & 1), kTcWaitTries);
-  } else {
-    const int row = 32 * wq + lane;
-    if (wg == 1) merge[row] = make_float2(m, s);
-    __syncthreads();
-    if (wg == 0) {
-      const float2 o = merge[row];
-      lse_merge(m, s, o.x, o.y);
-      part[(int64_t)sp * n_pad + (int64_t)t * 128 + row] = make_float2(m, s);
     }
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 128);
+  if (warp == 1) tc::tmem_dealloc(tmem, L::kTmemCols);
 }
 
 int tc_pack_points(const float* X, int64_t n, int64_t ldx, int d, int kp, __half* tiles, double* norm,
@@ -292,29 +384,20 @@ static cudaError_t tc_set_smem_attr() {
   return once;
 }
 
+// Resident CTAs per SM of the half-step kernel: one (576 threads, all of TMEM).
 int tc_ctas_per_sm(int kp) {
-  int n = 0;
-  if (kp == 32) {
-    if (tc_set_smem_attr<32>() != cudaSuccess) return 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lse_tc_kernel<32>, 256, TcSmem<32>::kAlloc) != cudaSuccess)
-      return 1;
-  } else {
-    if (tc_set_smem_attr<64>() != cudaSuccess) return 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lse_tc_kernel<64>, 256, TcSmem<64>::kAlloc) != cudaSuccess)
-      return 1;
-  }
-  return n > 0 ? n : 1;
+  (void)kp;
+  return 1;
 }
 
-int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nqt, const float* bias, int kp,
-                  float gamma, int nsplit, float2* part, int64_t n_pad, int* err, cudaStream_t st) {
-  dim3 grid((unsigned)nsplit, (unsigned)n_ptiles);
+int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, const float* bias, int kp,
+                  float gamma, int ctas, float2* part, int* err, cudaStream_t st) {
   if (kp == 32) {
     WOTG_CUDA(tc_set_smem_attr<32>());
-    lse_tc_kernel<32><<<grid, 256, TcSmem<32>::kAlloc, st>>>(Pt, Qt, bias, nqt, nsplit, gamma, part, n_pad, err);
+    lse_tc_kernel<32><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, bias, n_ptiles, nq, gamma, part, err);
   } else if (kp == 64) {
     WOTG_CUDA(tc_set_smem_attr<64>());
-    lse_tc_kernel<64><<<grid, 256, TcSmem<64>::kAlloc, st>>>(Pt, Qt, bias, nqt, nsplit, gamma, part, n_pad, err);
+    lse_tc_kernel<64><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, bias, n_ptiles, nq, gamma, part, err);
   } else {
     return WOTG_BADARG;
   }

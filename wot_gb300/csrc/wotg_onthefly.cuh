@@ -16,7 +16,19 @@ int tc_pack_points(const float* X, int64_t n, int64_t ldx, int d, int kp, __half
                    cudaStream_t st);
 // Resident CTAs per SM of the tensor-core half-step kernel.
 int tc_ctas_per_sm(int kp);
-int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nqt, const float* bias, int kp,
-                  float gamma, int nsplit, float2* part, int64_t n_pad, int* err, cudaStream_t st);
+// First flattened (row tile, column tile) index of CTA c's stretch, and the CTA
+// whose stretch holds index f, for `total` tiles cut into `ctas` stretches.
+__host__ __device__ __forceinline__ int64_t tc_stretch_begin(int64_t c, int64_t total, int64_t ctas) {
+  return c * total / ctas;
+}
+__host__ __device__ __forceinline__ int64_t tc_cta_of(int64_t f, int64_t total, int64_t ctas) {
+  return ((f + 1) * ctas - 1) / total;
+}
+
+// Persistent launch over n_ptiles x nq tile pairs with `ctas` CTAs; partial of
+// (CTA c, row tile t, row r, column quarter k) at part[((c + t) * 128 + r) * 4 + k]:
+// (ctas + n_ptiles) * 512 float2.
+int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, const float* bias, int kp,
+                  float gamma, int ctas, float2* part, int* err, cudaStream_t st);
 
 }  // namespace wotg

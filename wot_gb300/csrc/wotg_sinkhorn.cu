@@ -76,7 +76,7 @@ struct TcState {
   int kp;                   // packed dimension (32 or 64)
   int n_xt, n_yt;           // 128-point tiles of X and Y
   int64_t I_pad, J_pad;
-  int nsplit_row, nsplit_col;
+  int ctas_row, ctas_col;   // persistent grid of each pass
   __half* Xt;
   __half* Yt;
   double* normX;            // |x_i|^2 (FP64)
@@ -94,26 +94,40 @@ struct Geom {
   int64_t rows_per;
 };
 
-__device__ __forceinline__ void a_update(int64_t i, double L, const Vecs& V, const Coef& c,
-                                         unsigned long long* slot) {
+// The reference's a-update for row i; returns the new a_i (for the
+// absorption test, reduced per block by the caller).
+__device__ __forceinline__ double a_update(int64_t i, double L, const Vecs& V, const Coef& c) {
   const double ui = V.u[i];
   const double logs = ui * c.inv_eps + L - c.logJ;                 // log (K (b dy))_i
   const double la_new = c.alpha1 * (V.logp[i] - logs) - ui * c.inv_l1e;
   V.la_old[i] = V.la[i];
   V.la[i] = la_new;
   V.wrow[i] = (float)((ui * c.inv_eps + la_new) * kLog2e);
-  atomic_max_nonneg(slot, exp(la_new));
+  return exp(la_new);
 }
 
-__device__ __forceinline__ void b_update(int64_t j, double L, const Vecs& V, const Coef& c,
-                                         unsigned long long* slot) {
+__device__ __forceinline__ double b_update(int64_t j, double L, const Vecs& V, const Coef& c) {
   const double vj = V.v[j];
   const double logt = vj * c.inv_eps + L - c.logI;                 // log (K^T (a dx))_j
   const double lb_new = c.alpha2 * (c.logq - logt) - vj * c.inv_l2e;
   V.lb_old[j] = V.lb[j];
   V.lb[j] = lb_new;
   V.wcol[j] = (float)((vj * c.inv_eps + lb_new) * kLog2e);
-  atomic_max_nonneg(slot, exp(lb_new));
+  return exp(lb_new);
+}
+
+// Block-wide max of the threads' values, folded into the absorption slot with
+// one atomic per block (every thread of the block must call it).
+__device__ __forceinline__ void block_max_to_slot(double v, unsigned long long* slot) {
+  __shared__ double sh[32];
+  v = warp_maxd(v);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double w = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    w = warp_maxd(w);
+    if (threadIdx.x == 0) atomic_max_nonneg(slot, w);
+  }
 }
 
 // Row pass: one warp per row, 128-bit streaming loads of C, online base-2 LSE.
@@ -127,6 +141,7 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const float* __restrict__
   const int64_t nv = g.ldc >> 2;
   const float4* __restrict__ w4 = reinterpret_cast<const float4*>(V.wcol);
   const float k2 = c.kappa2;
+  double amax = 0.0;
   for (int64_t i = warp; i < g.I; i += nwarps) {
     const float4* __restrict__ row = reinterpret_cast<const float4*>(C + i * g.ldc);
     float m = kNegBig, s = 0.f;
@@ -163,16 +178,19 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const float* __restrict__
     if (lane == 0) {
       const double L = ((double)m + log2((double)s)) * kLn2;
       V.Lrow[i] = L;
-      if (UPDATE_A) a_update(i, L, V, c, V.maxslot + parity);
+      if (UPDATE_A) amax = fmax(amax, a_update(i, L, V, c));
     }
   }
+  if (UPDATE_A) block_max_to_slot(amax, V.maxslot + parity);
 }
 
 // a-update from a cached row LSE (the row pass of the preceding gap check).
 __global__ void a_update_kernel(Geom g, Vecs V, Coef c, int parity) {
+  double amax = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.I;
        i += (int64_t)gridDim.x * blockDim.x)
-    a_update(i, V.Lrow[i], V, c, V.maxslot + parity);
+    amax = fmax(amax, a_update(i, V.Lrow[i], V, c));
+  block_max_to_slot(amax, V.maxslot + parity);
 }
 
 // Column pass, phase 1: CTA = 1024 columns (float4 per thread) x rows_per rows;
@@ -239,17 +257,18 @@ __global__ void __launch_bounds__(256) col_partial_kernel(const float* __restric
 template <bool UPDATE_B>
 __global__ void col_combine_kernel(Geom g, Vecs V, Coef c, int parity) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= g.J) return;
-  float mx = kNegBig;
-  for (int r = 0; r < g.nrb; ++r) mx = fmaxf(mx, V.part[(int64_t)r * g.ldc + j].x);
-  double s = 0.0;
-  for (int r = 0; r < g.nrb; ++r) {
-    const float2 ps = V.part[(int64_t)r * g.ldc + j];
-    s += (double)ps.y * (double)ex2(ps.x - mx);
+  double bmax = 0.0;
+  if (j < g.J) {
+    float m = kNegBig, s = 0.f;
+    for (int r = 0; r < g.nrb; ++r) {
+      const float2 ps = V.part[(int64_t)r * g.ldc + j];
+      lse_merge(m, s, ps.x, ps.y);
+    }
+    const double L = ((double)m + log2((double)s)) * kLn2;
+    V.Lcol[j] = L;
+    if (UPDATE_B) bmax = b_update(j, L, V, c);
   }
-  const double L = ((double)mx + log2(s)) * kLn2;
-  V.Lcol[j] = L;
-  if (UPDATE_B) b_update(j, L, V, c, V.maxslot + parity);
+  if (UPDATE_B) block_max_to_slot(bmax, V.maxslot + parity);
 }
 
 // tau-absorption (optimal_transport.py:137-141 / :211-216): if max(a, b) > tau,
@@ -502,27 +521,39 @@ __global__ void tc_bias_kernel(int64_t n, int64_t n_pad, const double* __restric
     bias[i] = i < n ? (float)((pot[i] * inv_eps + lsc[i]) * kLog2e - kappa2d * norm[i]) : -INFINITY;
 }
 
+// Merge of the tensor-core kernel's partials: one thread per point, over the
+// (CTA, column quarter) partials whose stretch covered the point's row tile
+// (FP32 LSE merge), then the FP64 finish and update.
 template <bool ROW, bool UPDATE>
-__global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restrict__ part, int nsplit,
-                                  int64_t n_pad, const double* __restrict__ norm, int parity) {
+__global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restrict__ part, int nq, int ctas,
+                                  const double* __restrict__ norm, int parity) {
   const int64_t n = ROW ? g.I : g.J;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float mx = kNegBig;
-  for (int r = 0; r < nsplit; ++r) mx = fmaxf(mx, part[(int64_t)r * n_pad + i].x);
-  double s = 0.0;
-  for (int r = 0; r < nsplit; ++r) {
-    const float2 ps = part[(int64_t)r * n_pad + i];
-    s += (double)ps.y * (double)ex2(ps.x - mx);
+  double vmax = 0.0;
+  if (i < n) {
+    const int64_t t = i >> 7;
+    const int64_t total = (((n + 127) >> 7)) * (int64_t)nq;
+    const int64_t c_lo = tc_cta_of(t * nq, total, ctas);
+    const int64_t c_hi = tc_cta_of((t + 1) * nq - 1, total, ctas);
+    float m = kNegBig, s = 0.f;
+    for (int64_t cc = c_lo; cc <= c_hi; ++cc) {
+      const float4* p4 = reinterpret_cast<const float4*>(part + ((cc + t) * 128 + (i & 127)) * 4);
+      const float4 u0 = p4[0], u1 = p4[1];
+      lse_merge(m, s, u0.x, u0.y);
+      lse_merge(m, s, u0.z, u0.w);
+      lse_merge(m, s, u1.x, u1.y);
+      lse_merge(m, s, u1.z, u1.w);
+    }
+    const double L = ((double)m + log2((double)s)) * kLn2 - c.kappa * norm[i];
+    if (ROW) {
+      V.Lrow[i] = L;
+      if (UPDATE) vmax = a_update(i, L, V, c);
+    } else {
+      V.Lcol[i] = L;
+      if (UPDATE) vmax = b_update(i, L, V, c);
+    }
   }
-  const double L = ((double)mx + log2(s)) * kLn2 - c.kappa * norm[i];
-  if (ROW) {
-    V.Lrow[i] = L;
-    if (UPDATE) a_update(i, L, V, c, V.maxslot + parity);
-  } else {
-    V.Lcol[i] = L;
-    if (UPDATE) b_update(i, L, V, c, V.maxslot + parity);
-  }
+  if (UPDATE) block_max_to_slot(vmax, V.maxslot + parity);
 }
 
 // ---------------------------------------------------------------------------
@@ -564,11 +595,11 @@ struct Solver {
     tc_bias_kernel<<<vec_blocks(tc.J_pad), 256, 0, st>>>(g.J, tc.J_pad, V.v, V.lb, tc.normY, c.inv_eps,
                                                          c.kappa * kLog2e, tc.bias_row);
     WOTG_LAUNCHED();
-    int s = tc_lse_launch(tc.Xt, tc.n_xt, tc.Yt, tc.n_yt, tc.bias_row, tc.kp, 2.0f * c.kappa2, tc.nsplit_row,
-                          tc.part, tc.I_pad, tc.err, st);
+    int s = tc_lse_launch(tc.Xt, tc.n_xt, tc.Yt, tc.n_yt, tc.bias_row, tc.kp, 2.0f * c.kappa2, tc.ctas_row,
+                          tc.part, tc.err, st);
     if (s) return s;
-    tc_combine_kernel<true, UPDATE><<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, tc.part, tc.nsplit_row, tc.I_pad,
-                                                                     tc.normX, parity);
+    tc_combine_kernel<true, UPDATE><<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, tc.part, tc.n_yt, tc.ctas_row,
+                                                                          tc.normX, parity);
     WOTG_LAUNCHED();
     return WOTG_OK;
   }
@@ -576,11 +607,11 @@ struct Solver {
     tc_bias_kernel<<<vec_blocks(tc.I_pad), 256, 0, st>>>(g.I, tc.I_pad, V.u, V.la, tc.normX, c.inv_eps,
                                                          c.kappa * kLog2e, tc.bias_col);
     WOTG_LAUNCHED();
-    int s = tc_lse_launch(tc.Yt, tc.n_yt, tc.Xt, tc.n_xt, tc.bias_col, tc.kp, 2.0f * c.kappa2, tc.nsplit_col,
-                          tc.part, tc.J_pad, tc.err, st);
+    int s = tc_lse_launch(tc.Yt, tc.n_yt, tc.Xt, tc.n_xt, tc.bias_col, tc.kp, 2.0f * c.kappa2, tc.ctas_col,
+                          tc.part, tc.err, st);
     if (s) return s;
-    tc_combine_kernel<false, true><<<vec_blocks(g.J), 256, 0, st>>>(g, V, c, tc.part, tc.nsplit_col, tc.J_pad,
-                                                                    tc.normY, parity);
+    tc_combine_kernel<false, true><<<vec_blocks(g.J), 256, 0, st>>>(g, V, c, tc.part, tc.n_xt, tc.ctas_col,
+                                                                         tc.normY, parity);
     WOTG_LAUNCHED();
     return WOTG_OK;
   }
@@ -813,19 +844,29 @@ static int solve_fixed_iters(Solver& S, const wotg_params& P, double q, SolveRes
   return WOTG_OK;
 }
 
+// Resident 256-thread CTAs per SM of a kernel (6 when the query fails).
+template <class K>
+static int occupancy(K kernel) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, 256, 0) != cudaSuccess || n <= 0) return 6;
+  return n;
+}
+
 static Geom make_geom(int64_t I, int64_t J, int64_t ldc) {
   Geom g;
   g.I = I;
   g.J = J;
   g.ldc = ldc;
   const int sms = sm_count();
-  const int64_t max_warps = (int64_t)sms * 6 * 8;
+  static const int occ_row = occupancy(row_pass_kernel<true>);
+  static const int occ_col = occupancy(col_partial_kernel);
+  const int64_t max_warps = (int64_t)sms * occ_row * 8;
   const int64_t rows_per_warp = (I + max_warps - 1) / max_warps;
   const int64_t warps = (I + rows_per_warp - 1) / rows_per_warp;
   g.row_grid = (int)std::max<int64_t>(1, (warps + 7) / 8);
   const int64_t nv = ldc >> 2;
   g.ncb = (int)std::max<int64_t>(1, (nv + 255) / 256);
-  int64_t nrb = std::max<int64_t>(1, ((int64_t)sms * 6) / g.ncb);
+  int64_t nrb = std::max<int64_t>(1, ((int64_t)sms * occ_col) / g.ncb);
   nrb = std::min<int64_t>(nrb, std::max<int64_t>(1, I / 8));
   int64_t rows_per = (I + nrb - 1) / nrb;
   rows_per = (rows_per + kColRowChunk - 1) / kColRowChunk * kColRowChunk;
@@ -894,25 +935,6 @@ extern "C" int wotg_lse_matvec(const float* C, int64_t I, int64_t J, int64_t ldc
   return WOTG_OK;
 }
 
-// Split of the other set's tiles across CTAs that fills whole waves of the
-// tensor-core kernel as well as possible (ties: more CTAs).
-static int pick_nsplit(int row_tiles, int col_tiles, int slots) {
-  int best = 1;
-  double best_eff = -1.0;
-  const int cap = std::max(1, std::min(col_tiles, 64));
-  for (int ns = 1; ns <= cap; ++ns) {
-    const double ctas = (double)row_tiles * ns;
-    const double waves = std::ceil(ctas / slots);
-    double eff = ctas / (waves * slots);
-    if (ctas < slots) eff *= 0.5 + 0.5 * ctas / slots;
-    if (eff > best_eff + 1e-9 || (std::fabs(eff - best_eff) <= 1e-9 && ns > best)) {
-      best = ns;
-      best_eff = eff;
-    }
-  }
-  return best;
-}
-
 static bool tc_requested(const wotg_problem* prob) { return prob->form == WOTG_FORM_ONTHEFLY; }
 
 static int tc_valid(const wotg_problem* prob) {
@@ -930,8 +952,8 @@ static void tc_layout(Bump& b, const wotg_problem* prob, TcState& tc) {
   tc.I_pad = (int64_t)tc.n_xt * 128;
   tc.J_pad = (int64_t)tc.n_yt * 128;
   const int slots = sm_count() * std::max(1, tc_ctas_per_sm(tc.kp));
-  tc.nsplit_row = pick_nsplit(tc.n_xt, tc.n_yt, slots);
-  tc.nsplit_col = pick_nsplit(tc.n_yt, tc.n_xt, slots);
+  tc.ctas_row = (int)std::min<int64_t>(slots, (int64_t)tc.n_xt * tc.n_yt);
+  tc.ctas_col = (int)std::min<int64_t>(slots, (int64_t)tc.n_yt * tc.n_xt);
   const size_t tb = tc_tile_bytes(tc.kp);
   tc.Xt = reinterpret_cast<__half*>(b.take<unsigned char>(tb * tc.n_xt));
   tc.Yt = reinterpret_cast<__half*>(b.take<unsigned char>(tb * tc.n_yt));
@@ -939,7 +961,7 @@ static void tc_layout(Bump& b, const wotg_problem* prob, TcState& tc) {
   tc.normY = b.take<double>(prob->J);
   tc.bias_row = b.take<float>(tc.J_pad);
   tc.bias_col = b.take<float>(tc.I_pad);
-  tc.part = b.take<float2>(std::max((size_t)tc.nsplit_row * tc.I_pad, (size_t)tc.nsplit_col * tc.J_pad));
+  tc.part = b.take<float2>((size_t)(std::max(tc.ctas_row, tc.ctas_col) + std::max(tc.n_xt, tc.n_yt)) * 512);
   tc.err = b.take<int>(4);
 }
 
