@@ -13,7 +13,7 @@
 
 namespace wotg {
 
-constexpr uint32_t kTcWaitTries = 1u << 22;
+constexpr uint32_t kTcWaitTries = 4096;   // x up to 1 ms per try
 
 // ---------------------------------------------------------------------------
 // Self-test of the MMA path: D (128 x 128, FP32) = A (128 x 32) B (128 x 32)^T
@@ -91,12 +91,18 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const float* __restric
 
 
 // ---------------------------------------------------------------------------
-// Point packing (once per solve): each 128-point tile is stored as its FP16 hi
-// block then its lo block, K-major core-matrix layout with KP halfs per row
-// (dimensions beyond d and points beyond n are zero), plus FP64 |x|^2.
+// Point packing. Each 128-point tile is stored as its FP16 hi block then its
+// lo block, K-major core-matrix layout with KP halfs per row (x = hi + lo).
+// The MMA computes, per (row point p, column point q), the base-2 exponent
+//   sum_k a_k b_k = gamma (p . q) + bias_q
+// from two packings of the points:
+//   row form     a = [gamma x_1 .. gamma x_d, 1, 1, 0 ...]   (repacked per epsilon)
+//   column form  b = [x_1 .. x_d, beta1_q, beta2_q, 0 ...]   (bias columns per half-step)
+// where beta1 + beta2 carries the FP64 bias to ~44 bits (beta1 = fp32(bias),
+// beta2 = the remainder after beta1's hi/lo split). Points beyond n are zero.
 // ---------------------------------------------------------------------------
-__global__ void tc_pack_kernel(const float* __restrict__ X, int64_t n, int64_t ldx, int d, int kp,
-                               __half* __restrict__ tiles, double* __restrict__ norm) {
+__global__ void tc_pack_kernel(const float* __restrict__ X, int64_t n, int64_t ldx, int d, int kp, float scale,
+                               int row_form, __half* __restrict__ tiles, double* __restrict__ norm) {
   const int64_t ntiles = (n + 127) / 128;
   const int64_t total = ntiles * 128 * kp;
   const int64_t tile_halfs = (int64_t)2 * 128 * kp;
@@ -104,7 +110,9 @@ __global__ void tc_pack_kernel(const float* __restrict__ X, int64_t n, int64_t l
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = idx / kp;
     const int k = (int)(idx % kp);
-    const float x = (i < n && k < d) ? X[i * ldx + k] : 0.f;
+    float x = 0.f;
+    if (k < d) x = i < n ? scale * X[i * ldx + k] : 0.f;
+    else if (row_form && k < d + 2) x = 1.f;
     __half h, l;
     tc::split_f16(x, h, l);
     __half* tile = tiles + (i / 128) * tile_halfs;
@@ -112,23 +120,59 @@ __global__ void tc_pack_kernel(const float* __restrict__ X, int64_t n, int64_t l
     tile[off] = h;
     tile[128 * kp + off] = l;
   }
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int k = 0; k < d; ++k) {
-      const double x = X[i * ldx + k];
-      s += x * x;
+  if (norm) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      double s = 0.0;
+      for (int k = 0; k < d; ++k) {
+        const double x = X[i * ldx + k];
+        s += x * x;
+      }
+      norm[i] = s;
     }
-    norm[i] = s;
+  }
+}
+
+// Column-form bias columns of every point (and of the padding points):
+//   bias_q = (pot_q / eps + lsc_q) log2 e - kappa2 |q|^2
+// (-inf -> a large negative finite value, i.e. weight 0; NaN / +inf -> NaN so
+// that non-finite potentials propagate like in the materialised form).
+__global__ void tc_bias_pack_kernel(int64_t n, int64_t n_pad, const double* __restrict__ pot,
+                                    const double* __restrict__ lsc, const double* __restrict__ norm,
+                                    double inv_eps, double kappa2d, int d, int kp, __half* __restrict__ tiles) {
+  const int64_t tile_halfs = (int64_t)2 * 128 * kp;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += (int64_t)gridDim.x * blockDim.x) {
+    __half h1, l1, h2, l2;
+    const __half zero = __float2half_rn(0.f);
+    double beta = i < n ? (pot[i] * inv_eps + lsc[i]) * kLog2e - kappa2d * norm[i] : -INFINITY;
+    if (beta != beta || beta == INFINITY) {
+      h1 = __float2half_rn(NAN);
+      l1 = h2 = l2 = zero;
+    } else if (beta < -60000.0) {
+      h1 = __float2half_rn(-60000.f);
+      l1 = h2 = l2 = zero;
+    } else {
+      const float b1 = (float)beta;
+      tc::split_f16(b1, h1, l1);
+      const float b2 = (float)(beta - (double)__half2float(h1) - (double)__half2float(l1));
+      tc::split_f16(b2, h2, l2);
+    }
+    __half* tile = tiles + (i / 128) * tile_halfs;
+    const uint32_t o1 = tc::core_offset((int)(i % 128), d, kp) >> 1;
+    const uint32_t o2 = tc::core_offset((int)(i % 128), d + 1, kp) >> 1;
+    tile[o1] = h1;
+    tile[o2] = h2;
+    tile[128 * kp + o1] = l1;
+    tile[128 * kp + o2] = l2;
   }
 }
 
 // ---------------------------------------------------------------------------
 // On-the-fly half-step: base-2 log-sum-exp partials
 //   (m, s):  s 2^m = sum_j 2^(bias_j + gamma (p_i . q_j))
-// over 128-point tiles of the other set, where p . q comes from the FP16
-// split-precision MMA (hi.hi + hi.lo + lo.hi, FP32 accumulation in TMEM). The
-// row term of the exponent (-kappa |p_i|^2) and the FP64 merge of the partials
-// are applied by the caller.
+// over 128-point tiles of the other set. The whole exponent comes out of the
+// FP16 split-precision MMA (hi.hi + hi.lo + lo.hi, FP32 accumulation in TMEM)
+// of the row-form and column-form packings. The row term of the exponent
+// (-kappa |p_i|^2) and the FP64 merge of the partials are applied by the caller.
 //
 // Persistent schedule: the n_pt x nq (row tile, column tile) pairs are walked
 // row-major and cut into gridDim.x contiguous, equal stretches, one per CTA. A
@@ -144,22 +188,25 @@ __global__ void tc_pack_kernel(const float* __restrict__ X, int64_t n, int64_t l
 //   warp 1      MMA issuer: 6 split-precision MMAs per tile into one of four
 //               128 x 128 FP32 TMEM accumulators; owns the TMEM allocation;
 //   warps 2-17  epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 and the
-//               32 columns of quarter (w - 2) / 4, adds the column biases (read
-//               through L1) and folds them into a running (max, sum).
+//               32 columns of quarter (w - 2) / 4 and folds them into a
+//               running (max, sum).
 // mbarriers hand buffers between roles (full / empty per B stage, per A buffer
 // and per accumulator). Every wait is bounded: a role that times out sets *err
 // and stops; the others then time out in turn, and TMEM is freed at the end.
 // ---------------------------------------------------------------------------
-constexpr int kTcStages = 6;
-constexpr int kTcAcc = 4;            // TMEM accumulators (128 columns each)
-constexpr int kTcEpiWarps = 16;
+constexpr int kTcStages = 4;
+constexpr int kTcAcc = 2;            // TMEM accumulators (128 columns each)
+constexpr int kTcEpiWarps = 8;       // 4 x kTcParts: each reads one lane quarter x 128 / kTcParts columns
+constexpr int kTcParts = kTcEpiWarps / 4;
+constexpr int kTcColsPerWarp = 128 / kTcParts;
+constexpr int kTcCtasPerSm = 2;
 constexpr int kTcThreads = 32 * (2 + kTcEpiWarps);
 
 template <int KP>
 struct TcSmem {
   static constexpr uint32_t kHalfBytes = 128u * KP * 2u;      // one of hi / lo
   static constexpr uint32_t kTileBytes = 2u * kHalfBytes;      // packed 128-point tile (hi + lo)
-  static constexpr int kStages = KP == 32 ? kTcStages : 2;     // B ring depth (shared-memory budget)
+  static constexpr int kStages = KP == 32 ? kTcStages : 1;     // B ring depth (shared-memory budget)
   static constexpr uint32_t kA = 0;                            // 2 buffers
   static constexpr uint32_t kB = 2 * kTileBytes;               // kStages buffers
   static constexpr uint32_t kBar = kB + kStages * kTileBytes;
@@ -187,18 +234,12 @@ __device__ __forceinline__ void tc_issue_mma(uint32_t tmem_d, uint32_t sAt, uint
   }
 }
 
-// Online LSE of 32 exponents gamma * d[c] + b[c] into (m, s): packed FP32x2
-// arithmetic and tree reductions.
-__device__ __forceinline__ void lse32(const float (&d)[32], const float4* __restrict__ b4, float gamma, float& m,
-                                      float& s) {
+// Online LSE of 32 exponents d[c] into (m, s): packed FP32x2 arithmetic and
+// tree reductions.
+__device__ __forceinline__ void lse32(const float (&d)[32], float& m, float& s) {
   float2 x[16];
-  const float2 g2 = make_float2(gamma, gamma);
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const float4 b = __ldg(b4 + c);
-    x[2 * c] = __ffma2_rn(g2, make_float2(d[4 * c], d[4 * c + 1]), make_float2(b.x, b.y));
-    x[2 * c + 1] = __ffma2_rn(g2, make_float2(d[4 * c + 2], d[4 * c + 3]), make_float2(b.z, b.w));
-  }
+  for (int c = 0; c < 16; ++c) x[c] = make_float2(d[2 * c], d[2 * c + 1]);
   float mx[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) mx[c] = fmaxf(fmaxf(x[2 * c].x, x[2 * c].y), fmaxf(x[2 * c + 1].x, x[2 * c + 1].y));
@@ -223,10 +264,9 @@ __device__ __forceinline__ void lse32(const float (&d)[32], const float4* __rest
 }
 
 template <int KP>
-__global__ void __launch_bounds__(kTcThreads, 1) lse_tc_kernel(const __half* __restrict__ Pt,
+__global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const __half* __restrict__ Pt,
                                                                const __half* __restrict__ Qt,
-                                                               const float* __restrict__ bias, int n_pt, int nq,
-                                                               float gamma, float2* __restrict__ part,
+                                                               int n_pt, int nq, float2* __restrict__ part,
                                                                int* __restrict__ err) {
   using L = TcSmem<KP>;
   constexpr int S = L::kStages;
@@ -306,32 +346,64 @@ __global__ void __launch_bounds__(kTcThreads, 1) lse_tc_kernel(const __half* __r
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      // MMA issuer
+      // MMA issuer. The 6 MMAs of a tile accumulate into one TMEM accumulator and
+      // so run one after another; tiles are therefore issued in pairs with their
+      // MMAs interleaved, giving the tensor core two independent chains.
       int q = q_first, seg = 0;
-      for (int j = 0; j < n; ++j) {
-        const int stage = j % S, b = j % kTcAcc;
-        const bool new_seg = j == 0 || q == 0;
-        if (new_seg && j > 0) ++seg;
+      constexpr int kGroup = kTcAcc >= 4 ? 2 : 1;
+      for (int j0 = 0; j0 < n; j0 += kGroup) {
+        const int cnt = j0 + 1 < n ? kGroup : 1;
+        uint32_t a_addr[kGroup], b_addr[kGroup], d_addr[kGroup];
+        bool seg_end[kGroup];
+        int seg_of[kGroup];
         bool good = true;
-        if (new_seg) good = tc::mbar_wait(&a_full[seg & 1], (uint32_t)((seg >> 1) & 1), kTcWaitTries);
-        good = good && tc::mbar_wait(&full[stage], (uint32_t)((j / S) & 1), kTcWaitTries);
-        if (j >= kTcAcc)
-          good = good && tc::mbar_wait(&acc_empty[b], (uint32_t)((j / kTcAcc - 1) & 1), kTcWaitTries);
+        for (int u = 0; u < cnt; ++u) {
+          const int j = j0 + u;
+          const int stage = j % S, b = j % kTcAcc;
+          const bool new_seg = j == 0 || q == 0;
+          if (new_seg && j > 0) ++seg;
+          if (new_seg) good = good && tc::mbar_wait(&a_full[seg & 1], (uint32_t)((seg >> 1) & 1), kTcWaitTries);
+          good = good && tc::mbar_wait(&full[stage], (uint32_t)((j / S) & 1), kTcWaitTries);
+          if (j >= kTcAcc)
+            good = good && tc::mbar_wait(&acc_empty[b], (uint32_t)((j / kTcAcc - 1) & 1), kTcWaitTries);
+          a_addr[u] = sA + (uint32_t)(seg & 1) * L::kTileBytes;
+          b_addr[u] = sB + (uint32_t)stage * L::kTileBytes;
+          d_addr[u] = tmem + (uint32_t)(128 * b);
+          seg_of[u] = seg;
+          if (++q == nq) q = 0;
+          seg_end[u] = j == n - 1 || q == 0;
+        }
         if (!good) {
           atomicExch(err, 1);
           break;
         }
         tc::fence_after_sync();
-        tc_issue_mma<KP>(tmem + (uint32_t)(128 * b), sA + (uint32_t)(seg & 1) * L::kTileBytes,
-                         sB + (uint32_t)stage * L::kTileBytes);
-        tc::mma_commit(&empty[stage]);
-        tc::mma_commit(&acc_full[b]);
-        if (++q == nq) q = 0;
-        if (j == n - 1 || q == 0) tc::mma_commit(&a_empty[seg & 1]);
+        constexpr uint32_t idesc = tc::idesc_f16_f32(128, 128);
+        constexpr uint32_t sbo = KP * 16;
+#pragma unroll
+        for (int st = 0; st < KP / 16; ++st) {
+          const uint32_t ko = (uint32_t)st * 2u * tc::kCoreLbo;
+#pragma unroll
+          for (int pr = 0; pr < 3; ++pr) {
+            for (int u = 0; u < cnt; ++u) {
+              const uint32_t a_off = pr == 2 ? L::kHalfBytes : 0u;   // lo.hi uses A lo
+              const uint32_t b_off = pr == 1 ? L::kHalfBytes : 0u;   // hi.lo uses B lo
+              tc::mma_f16(d_addr[u], tc::smem_desc(a_addr[u] + a_off + ko, tc::kCoreLbo, sbo),
+                          tc::smem_desc(b_addr[u] + b_off + ko, tc::kCoreLbo, sbo), idesc,
+                          (st > 0 || pr > 0) ? 1u : 0u);
+            }
+          }
+        }
+        for (int u = 0; u < cnt; ++u) {
+          const int j = j0 + u;
+          tc::mma_commit(&empty[j % S]);
+          tc::mma_commit(&acc_full[j % kTcAcc]);
+          if (seg_end[u]) tc::mma_commit(&a_empty[seg_of[u] & 1]);
+        }
       }
     }
   } else {
-    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, columns of quarter (w - 2) / 4
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, columns of group (w - 2) / 4
     const int wq = warp & 3, cq = (warp - 2) >> 2;
     const int row = 32 * wq + lane;
     float m = kNegBig, s = 0.f;
@@ -345,15 +417,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) lse_tc_kernel(const __half* __r
         break;
       }
       tc::fence_after_sync();
-      float d[32];
-      tc::tmem_ld32(tmem + ((uint32_t)(32 * wq) << 16) + (uint32_t)(128 * b + 32 * cq), d);
+      float d[kTcColsPerWarp];
+#pragma unroll
+      for (int h = 0; h < kTcColsPerWarp / 32; ++h)
+        tc::tmem_ld32(tmem + ((uint32_t)(32 * wq) << 16) + (uint32_t)(128 * b + kTcColsPerWarp * cq + 32 * h),
+                      *reinterpret_cast<float(*)[32]>(&d[32 * h]));
       tc::tmem_wait_ld();
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
-      lse32(d, reinterpret_cast<const float4*>(bias + (int64_t)q * 128 + 32 * cq), gamma, m, s);
+#pragma unroll
+      for (int h = 0; h < kTcColsPerWarp / 32; ++h) lse32(*reinterpret_cast<float(*)[32]>(&d[32 * h]), m, s);
       if (++q == nq || j == n - 1) {
-        part[(((int64_t)blockIdx.x + t) * 128 + row) * 4 + cq] = make_float2(m, s);
+        part[(((int64_t)blockIdx.x + t) * 128 + row) * kTcParts + cq] = make_float2(m, s);
         m = kNegBig;
         s = 0.f;
         if (q == nq) {
@@ -368,11 +444,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) lse_tc_kernel(const __half* __r
   if (warp == 1) tc::tmem_dealloc(tmem, L::kTmemCols);
 }
 
-int tc_pack_points(const float* X, int64_t n, int64_t ldx, int d, int kp, __half* tiles, double* norm,
-                   cudaStream_t st) {
+int tc_pack_points(const float* X, int64_t n, int64_t ldx, int d, int kp, float scale, int row_form,
+                   __half* tiles, double* norm, cudaStream_t st) {
   const int64_t total = (n + 127) / 128 * 128 * kp;
   const int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sm_count() * 8);
-  tc_pack_kernel<<<grid, 256, 0, st>>>(X, n, ldx, d, kp, tiles, norm);
+  tc_pack_kernel<<<grid, 256, 0, st>>>(X, n, ldx, d, kp, scale, row_form, tiles, norm);
+  WOTG_LAUNCHED();
+  return WOTG_OK;
+}
+
+int tc_pack_bias(int64_t n, const double* pot, const double* lsc, const double* norm, double inv_eps,
+                 double kappa2d, int d, int kp, __half* tiles, cudaStream_t st) {
+  const int64_t n_pad = (n + 127) / 128 * 128;
+  const int grid = (int)std::min<int64_t>((n_pad + 255) / 256, (int64_t)sm_count() * 8);
+  tc_bias_pack_kernel<<<grid, 256, 0, st>>>(n, n_pad, pot, lsc, norm, inv_eps, kappa2d, d, kp, tiles);
   WOTG_LAUNCHED();
   return WOTG_OK;
 }
@@ -384,20 +469,18 @@ static cudaError_t tc_set_smem_attr() {
   return once;
 }
 
-// Resident CTAs per SM of the half-step kernel: one (576 threads, all of TMEM).
-int tc_ctas_per_sm(int kp) {
-  (void)kp;
-  return 1;
-}
+// Resident CTAs per SM of the half-step kernel.
+int tc_ctas_per_sm(int kp) { return kp == 32 ? kTcCtasPerSm : 1; }
+int tc_parts() { return kTcParts; }
 
-int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, const float* bias, int kp,
-                  float gamma, int ctas, float2* part, int* err, cudaStream_t st) {
+int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int kp, int ctas, float2* part,
+                  int* err, cudaStream_t st) {
   if (kp == 32) {
     WOTG_CUDA(tc_set_smem_attr<32>());
-    lse_tc_kernel<32><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, bias, n_ptiles, nq, gamma, part, err);
+    lse_tc_kernel<32><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, err);
   } else if (kp == 64) {
     WOTG_CUDA(tc_set_smem_attr<64>());
-    lse_tc_kernel<64><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, bias, n_ptiles, nq, gamma, part, err);
+    lse_tc_kernel<64><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, err);
   } else {
     return WOTG_BADARG;
   }

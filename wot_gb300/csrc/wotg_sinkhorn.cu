@@ -77,12 +77,16 @@ struct TcState {
   int n_xt, n_yt;           // 128-point tiles of X and Y
   int64_t I_pad, J_pad;
   int ctas_row, ctas_col;   // persistent grid of each pass
-  __half* Xt;
-  __half* Yt;
+  __half* Xa;               // row form of X: [gamma x, 1, 1]   (repacked per epsilon)
+  __half* Xb;               // column form of X: [x, bias columns] (bias per half-step)
+  __half* Ya;
+  __half* Yb;
+  const float* X;
+  const float* Y;
+  int64_t ldx, ldy;
+  int d;
   double* normX;            // |x_i|^2 (FP64)
   double* normY;
-  float* bias_row;          // J_pad: bias over columns for the row pass
-  float* bias_col;          // I_pad: bias over rows for the column pass
   float2* part;
   int* err;
 };
@@ -508,25 +512,19 @@ __global__ void __launch_bounds__(256) coupling_kernel(const float* __restrict__
 }
 
 // ---------------------------------------------------------------------------
-// On-the-fly form: per-half-step biases and the FP64 merge of the tensor-core
-// kernel's partials. The exponent of element (i, j) is split as
+// On-the-fly form: the FP64 merge of the tensor-core kernel's partials. The
+// exponent of element (i, j) is split as
 //   bias_j + gamma (x_i . y_j) - kappa2 |x_i|^2,   gamma = 2 kappa2,
-//   bias_j = (v_j / eps + lb_j) log2 e - kappa2 |y_j|^2     (FP64, rounded once),
-// i.e. (v_j/eps + lb_j - kappa C_ij) in base 2 with C = |x|^2 + |y|^2 - 2 x.y.
+//   bias_j = (v_j / eps + lb_j) log2 e - kappa2 |y_j|^2     (FP64, carried by the MMA),
+// i.e. (v_j/eps + lb_j - kappa C_ij) in base 2 with C = |x|^2 + |y|^2 - 2 x.y; the
+// tensor-core kernel produces the first two terms, the merge adds the third.
 // ---------------------------------------------------------------------------
-__global__ void tc_bias_kernel(int64_t n, int64_t n_pad, const double* __restrict__ pot,
-                               const double* __restrict__ lsc, const double* __restrict__ norm, double inv_eps,
-                               double kappa2d, float* __restrict__ bias) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += (int64_t)gridDim.x * blockDim.x)
-    bias[i] = i < n ? (float)((pot[i] * inv_eps + lsc[i]) * kLog2e - kappa2d * norm[i]) : -INFINITY;
-}
-
 // Merge of the tensor-core kernel's partials: one thread per point, over the
 // (CTA, column quarter) partials whose stretch covered the point's row tile
 // (FP32 LSE merge), then the FP64 finish and update.
 template <bool ROW, bool UPDATE>
 __global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restrict__ part, int nq, int ctas,
-                                  const double* __restrict__ norm, int parity) {
+                                  int nparts, const double* __restrict__ norm, int parity) {
   const int64_t n = ROW ? g.I : g.J;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double vmax = 0.0;
@@ -537,12 +535,11 @@ __global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restri
     const int64_t c_hi = tc_cta_of((t + 1) * nq - 1, total, ctas);
     float m = kNegBig, s = 0.f;
     for (int64_t cc = c_lo; cc <= c_hi; ++cc) {
-      const float4* p4 = reinterpret_cast<const float4*>(part + ((cc + t) * 128 + (i & 127)) * 4);
-      const float4 u0 = p4[0], u1 = p4[1];
-      lse_merge(m, s, u0.x, u0.y);
-      lse_merge(m, s, u0.z, u0.w);
-      lse_merge(m, s, u1.x, u1.y);
-      lse_merge(m, s, u1.z, u1.w);
+      const float2* pp = part + ((cc + t) * 128 + (i & 127)) * nparts;
+      for (int k = 0; k < nparts; ++k) {
+        const float2 u = pp[k];
+        lse_merge(m, s, u.x, u.y);
+      }
     }
     const double L = ((double)m + log2((double)s)) * kLn2 - c.kappa * norm[i];
     if (ROW) {
@@ -590,28 +587,36 @@ struct Solver {
   int vec_blocks(int64_t n) const { return (int)std::max<int64_t>(1, (n + 255) / 256); }
 
   // On-the-fly row pass (K (b dy)) / column pass (K^T (a dx)).
+  // Row forms carry gamma = 2 kappa2, which changes with epsilon. Column forms
+  // hold sqrt(cost_scale) y and row forms (gamma / sqrt(cost_scale)) x, so that
+  // both stay in median-normalised units whatever the units of the input points
+  // (FP16 range); their product is gamma x . y.
+  int tc_prepare(const Coef& c) {
+    if (!tc.on) return WOTG_OK;
+    const float gamma = (float)(2.0 * c.kappa * kLog2e / std::sqrt(cost_scale));
+    int s = tc_pack_points(tc.X, g.I, tc.ldx, tc.d, tc.kp, gamma, 1, tc.Xa, nullptr, st);
+    if (s) return s;
+    return tc_pack_points(tc.Y, g.J, tc.ldy, tc.d, tc.kp, gamma, 1, tc.Ya, nullptr, st);
+  }
+
   template <bool UPDATE>
   int tc_row_pass(const Coef& c, int parity) {
-    tc_bias_kernel<<<vec_blocks(tc.J_pad), 256, 0, st>>>(g.J, tc.J_pad, V.v, V.lb, tc.normY, c.inv_eps,
-                                                         c.kappa * kLog2e, tc.bias_row);
-    WOTG_LAUNCHED();
-    int s = tc_lse_launch(tc.Xt, tc.n_xt, tc.Yt, tc.n_yt, tc.bias_row, tc.kp, 2.0f * c.kappa2, tc.ctas_row,
-                          tc.part, tc.err, st);
+    int s = tc_pack_bias(g.J, V.v, V.lb, tc.normY, c.inv_eps, c.kappa * kLog2e, tc.d, tc.kp, tc.Yb, st);
+    if (s) return s;
+    s = tc_lse_launch(tc.Xa, tc.n_xt, tc.Yb, tc.n_yt, tc.kp, tc.ctas_row, tc.part, tc.err, st);
     if (s) return s;
     tc_combine_kernel<true, UPDATE><<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, tc.part, tc.n_yt, tc.ctas_row,
-                                                                          tc.normX, parity);
+                                                                          tc_parts(), tc.normX, parity);
     WOTG_LAUNCHED();
     return WOTG_OK;
   }
   int tc_col_pass(const Coef& c, int parity) {
-    tc_bias_kernel<<<vec_blocks(tc.I_pad), 256, 0, st>>>(g.I, tc.I_pad, V.u, V.la, tc.normX, c.inv_eps,
-                                                         c.kappa * kLog2e, tc.bias_col);
-    WOTG_LAUNCHED();
-    int s = tc_lse_launch(tc.Yt, tc.n_yt, tc.Xt, tc.n_xt, tc.bias_col, tc.kp, 2.0f * c.kappa2, tc.ctas_col,
-                          tc.part, tc.err, st);
+    int s = tc_pack_bias(g.I, V.u, V.la, tc.normX, c.inv_eps, c.kappa * kLog2e, tc.d, tc.kp, tc.Xb, st);
+    if (s) return s;
+    s = tc_lse_launch(tc.Ya, tc.n_yt, tc.Xb, tc.n_xt, tc.kp, tc.ctas_col, tc.part, tc.err, st);
     if (s) return s;
     tc_combine_kernel<false, true><<<vec_blocks(g.J), 256, 0, st>>>(g, V, c, tc.part, tc.n_xt, tc.ctas_col,
-                                                                         tc.normY, parity);
+                                                                         tc_parts(), tc.normY, parity);
     WOTG_LAUNCHED();
     return WOTG_OK;
   }
@@ -740,6 +745,8 @@ static int solve_duality_gap(Solver& S, const wotg_params& P, double q, SolveRes
     c = S.coef(eps_i, P, q);
     int s = S.rescale(eps_old, eps_i);
     if (s) return s;
+    s = S.tc_prepare(c);
+    if (s) return s;
     parity = 0;
     lrow_valid = false;
     const bool final = stage == n_scalings;
@@ -812,6 +819,8 @@ static int solve_fixed_iters(Solver& S, const wotg_params& P, double q, SolveRes
   Coef c = S.coef(eps_i, P, q);
   int s = S.rescale(0.0, eps_i);
   if (s) return s;
+  s = S.tc_prepare(c);
+  if (s) return s;
   int parity = 0;
   int since = 0, index = 0;
   for (int it = 0; it < P.scaling_iter; ++it) {
@@ -830,6 +839,8 @@ static int solve_fixed_iters(Solver& S, const wotg_params& P, double q, SolveRes
       parity = 0;
       eps_i = eps_new;
       c = S.coef(eps_i, P, q);
+      s = S.tc_prepare(c);
+      if (s) return s;
     }
   }
   for (int it = 0; it < P.extra_iter; ++it) {
@@ -939,7 +950,8 @@ static bool tc_requested(const wotg_problem* prob) { return prob->form == WOTG_F
 
 static int tc_valid(const wotg_problem* prob) {
   if (!tc_requested(prob)) return prob->form == WOTG_FORM_MATERIALIZED ? WOTG_OK : WOTG_BADARG;
-  if (!prob->X || !prob->Y || prob->d < 1 || prob->d > 64 || prob->ldx < prob->d || prob->ldy < prob->d)
+  if (!(prob->cost_scale > 0)) return WOTG_BADARG;
+  if (!prob->X || !prob->Y || prob->d < 1 || prob->d > tc_max_dim() || prob->ldx < prob->d || prob->ldy < prob->d)
     return WOTG_BADARG;
   return WOTG_OK;
 }
@@ -955,13 +967,19 @@ static void tc_layout(Bump& b, const wotg_problem* prob, TcState& tc) {
   tc.ctas_row = (int)std::min<int64_t>(slots, (int64_t)tc.n_xt * tc.n_yt);
   tc.ctas_col = (int)std::min<int64_t>(slots, (int64_t)tc.n_yt * tc.n_xt);
   const size_t tb = tc_tile_bytes(tc.kp);
-  tc.Xt = reinterpret_cast<__half*>(b.take<unsigned char>(tb * tc.n_xt));
-  tc.Yt = reinterpret_cast<__half*>(b.take<unsigned char>(tb * tc.n_yt));
+  tc.Xa = reinterpret_cast<__half*>(b.take<unsigned char>(tb * tc.n_xt));
+  tc.Xb = reinterpret_cast<__half*>(b.take<unsigned char>(tb * tc.n_xt));
+  tc.Ya = reinterpret_cast<__half*>(b.take<unsigned char>(tb * tc.n_yt));
+  tc.Yb = reinterpret_cast<__half*>(b.take<unsigned char>(tb * tc.n_yt));
+  tc.X = prob->X;
+  tc.Y = prob->Y;
+  tc.ldx = prob->ldx;
+  tc.ldy = prob->ldy;
+  tc.d = prob->d;
   tc.normX = b.take<double>(prob->I);
   tc.normY = b.take<double>(prob->J);
-  tc.bias_row = b.take<float>(tc.J_pad);
-  tc.bias_col = b.take<float>(tc.I_pad);
-  tc.part = b.take<float2>((size_t)(std::max(tc.ctas_row, tc.ctas_col) + std::max(tc.n_xt, tc.n_yt)) * 512);
+  tc.part = b.take<float2>((size_t)(std::max(tc.ctas_row, tc.ctas_col) + std::max(tc.n_xt, tc.n_yt)) * 128 *
+                           tc_parts());
   tc.err = b.take<int>(4);
 }
 
@@ -1021,9 +1039,11 @@ extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wot
   if (tc_requested(prob)) {
     tc_layout(b, prob, S.tc);
     WOTG_CUDA(cudaMemsetAsync(S.tc.err, 0, sizeof(int), st));
-    int s = tc_pack_points(prob->X, I, prob->ldx, prob->d, S.tc.kp, S.tc.Xt, S.tc.normX, st);
+    // column forms (coordinates; bias columns written per half-step) and norms
+    const float sigma = (float)std::sqrt(prob->cost_scale);
+    int s = tc_pack_points(prob->X, I, prob->ldx, prob->d, S.tc.kp, sigma, 0, S.tc.Xb, S.tc.normX, st);
     if (s) return s;
-    s = tc_pack_points(prob->Y, J, prob->ldy, prob->d, S.tc.kp, S.tc.Yt, S.tc.normY, st);
+    s = tc_pack_points(prob->Y, J, prob->ldy, prob->d, S.tc.kp, sigma, 0, S.tc.Yb, S.tc.normY, st);
     if (s) return s;
   }
 

@@ -62,17 +62,20 @@ __device__ __forceinline__ void mbar_fence_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Bounded wait for the completion of phase `parity` of an mbarrier. Returns
-// false after `max_tries` unsuccessful polls (each try_wait may itself block for
-// a short, hardware-defined time), so a wait can never hang the kernel.
+// Bounded wait for the completion of phase `parity` of an mbarrier. Each
+// try_wait suspends the thread until the phase completes or kSuspendNs
+// nanoseconds pass (so waiting warps sleep instead of polling shared memory);
+// after `max_tries` unsuccessful tries (~max_tries ms) it returns false, so a
+// wait can never hang the kernel.
+constexpr uint32_t kSuspendNs = 1000000;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_tries) {
   const uint32_t addr = smem_u32(bar);
   for (uint32_t t = 0; t < max_tries; ++t) {
     uint32_t done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
         : "=r"(done)
-        : "r"(addr), "r"(parity)
+        : "r"(addr), "r"(parity), "r"(kSuspendNs)
         : "memory");
     if (done) return true;
   }
