@@ -46,7 +46,7 @@ def parse():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--pair', default=None, help='I,J cells of a smaller pair (profiling runs)')
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--form', default='materialized', choices=['materialized', 'onthefly', 'auto'],
+    ap.add_argument('--form', default='auto', choices=['materialized', 'onthefly', 'auto'],
                     help='materialised FP32 cost stream or tensor-core cost recomputation')
     return ap.parse_args()
 
@@ -56,12 +56,13 @@ def dist_env():
 
 
 def peaks():
+    """(HBM GB/s, dense bf16 TFLOP/s, 'measured' | 'fallback')."""
     try:
         with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
             p = json.load(f)
-        return float(p['hbm_gbs']), 'measured'
+        return float(p['hbm_gbs']), float(p['bf16_tflops']), 'measured'
     except Exception:
-        return 6800.0, 'fallback'
+        return 6800.0, 1900.0, 'fallback'
 
 
 class Clocks:
@@ -246,42 +247,62 @@ def main():
         t = float(tt.item())
     value = world * args.steps / t
 
-    # dominant kernel: the streaming row half-step over the FP32 cost
+    # dominant kernels, timed live with CUDA events on the launching stream
+    import ctypes
     cost = D.default_cost(a, b)
+    form = D.resolve_form(cost, args.form)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    reps = 20
+
+    def time_launches(fn):
+        for _ in range(3):
+            fn()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps)]
+        for r in range(reps):
+            evs[2 * r].record(stream)
+            fn()
+            evs[2 * r + 1].record(stream)
+        torch.cuda.synchronize()
+        return float(np.mean([evs[2 * r].elapsed_time(evs[2 * r + 1]) for r in range(reps)])) / 1e3
+
+    hbm_peak, tf_peak, peak_kind = peaks()
+    # materialised form: streaming row pass over the FP32 cost (HBM-bound)
     ldc = cost.ldc
     w = torch.zeros(ldc, dtype=torch.float32, device='cuda')
     L = torch.empty(I_FULL, dtype=torch.float64, device='cuda')
     L2 = torch.empty(J_FULL, dtype=torch.float64, device='cuda')
     wr = torch.zeros(I_FULL, dtype=torch.float32, device='cuda')
     ws = torch.empty(lib.wotg_lse_matvec_workspace_bytes(I_FULL, J_FULL, ldc), dtype=torch.uint8, device='cuda')
-    import ctypes
-    sh = ctypes.c_void_p(stream.cuda_stream)
     k2 = ctypes.c_float(float(cost.scale / CFG['epsilon'] * 1.4426950408889634))
-    reps = 20
-    durs = {}
-    for axis, wv, Lv in ((0, w, L), (1, wr, L2)):
-        for _ in range(3):
-            lib.wotg_lse_matvec(cost.C.data_ptr(), I_FULL, J_FULL, ldc, wv.data_ptr(), k2, axis, Lv.data_ptr(),
-                                ws.data_ptr(), ws.numel(), sh)
-        evs = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps)]
-        for r in range(reps):
-            evs[2 * r].record(stream)
-            st = lib.wotg_lse_matvec(cost.C.data_ptr(), I_FULL, J_FULL, ldc, wv.data_ptr(), k2, axis,
-                                     Lv.data_ptr(), ws.data_ptr(), ws.numel(), sh)
-            evs[2 * r + 1].record(stream)
-            assert st == 0
-        torch.cuda.synchronize()
-        durs[axis] = float(np.mean([evs[2 * r].elapsed_time(evs[2 * r + 1]) for r in range(reps)])) / 1e3
+    t_row = time_launches(lambda: lib.wotg_lse_matvec(cost.C.data_ptr(), I_FULL, J_FULL, ldc, w.data_ptr(), k2, 0,
+                                                      L.data_ptr(), ws.data_ptr(), ws.numel(), sh))
+    t_col = time_launches(lambda: lib.wotg_lse_matvec(cost.C.data_ptr(), I_FULL, J_FULL, ldc, wr.data_ptr(), k2, 1,
+                                                      L2.data_ptr(), ws.data_ptr(), ws.numel(), sh))
     alg_bytes = I_FULL * J_FULL * 4 + (J_FULL + I_FULL) * 12
-    peak, peak_kind = peaks()
-    achieved = alg_bytes / durs[0] / 1e9
     # DRAM bytes read + written per algorithmic byte of the row pass, from an ncu
     # capture of the same kernel on an 8000 x 10000 pair (traffic grows with I*J)
     traffic_ratio = (320.801280 + 3.477504) / (8000 * 10000 * 4 / 1e6)
-    roofline = {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
-                'traffic': I_FULL * J_FULL * 4 * traffic_ratio, 'kernel': 'row_pass_kernel (wotg_lse_matvec axis 0)', 'peak_kind': peak_kind,
-                'col_pass_GBps': alg_bytes / durs[1] / 1e9,
-                'row_pass_ms': durs[0] * 1e3, 'col_pass_ms': durs[1] * 1e3}
+    roof_mat = {'bound': 'hbm', 'achieved': alg_bytes / t_row / 1e9, 'peak': hbm_peak, 'unit': 'GB/s',
+                'frac': alg_bytes / t_row / 1e9 / hbm_peak, 'traffic': I_FULL * J_FULL * 4 * traffic_ratio,
+                'kernel': 'row_pass_kernel (wotg_lse_matvec axis 0)', 'peak_kind': peak_kind,
+                'row_pass_ms': t_row * 1e3, 'col_pass_ms': t_col * 1e3,
+                'col_pass_GBps': alg_bytes / t_col / 1e9}
+    # on-the-fly form: tensor-core half-step from the points
+    wj = torch.zeros(J_FULL, dtype=torch.float64, device='cuda')
+    wsp = torch.empty(lib.wotg_lse_points_workspace_bytes(I_FULL, J_FULL, PCA_D), dtype=torch.uint8, device='cuda')
+    sc = float(cost.scale / CFG['epsilon'])
+    t_tc = time_launches(lambda: lib.wotg_lse_points(a.data_ptr(), I_FULL, a.stride(0), b.data_ptr(), J_FULL,
+                                                     b.stride(0), PCA_D, sc, wj.data_ptr(), L.data_ptr(),
+                                                     wsp.data_ptr(), wsp.numel(), sh))
+    flops = 2.0 * PCA_D * I_FULL * J_FULL           # algorithmic cross-term contraction
+    roof_tc = {'bound': 'tensor', 'achieved': flops / t_tc / 1e12, 'peak': tf_peak, 'unit': 'TFLOP/s',
+               'frac': flops / t_tc / 1e12 / tf_peak, 'traffic': None,
+               'kernel': 'lse_tc_kernel (wotg_lse_points)', 'peak_kind': peak_kind, 'launch_ms': t_tc * 1e3,
+               'executed_mma_tflops': 3 * 2.0 * 32 * I_FULL * J_FULL / t_tc / 1e12,
+               'exp_per_s': I_FULL * J_FULL / t_tc,
+               'note': 'the exp + FP32 reduction of every cost element (one per element, from TMEM) bounds this '
+                       'kernel, not the split-precision MMA (3 FP16 products per contraction step)'}
+    roofline = roof_tc if form == _native.FORM_ONTHEFLY else roof_mat
     del cost
 
     line = {'metric': METRIC, 'value': value, 'unit': 'maps/s', 'n_gpus': world, 'steps': args.steps,
@@ -291,7 +312,9 @@ def main():
                        'l2': 'inputs larger than L2 (FP32 cost 2.0 GB per pass)',
                        'timed': 'cost + median + 3 duality-gap solves + dense FP64 coupling, coordinates resident'},
             'sinkhorn_iter_per_s': iters / t * world, 'iterations_per_map': iters / args.steps,
-            'roofline': roofline, 'gpu_launches': int(launches), 'clocks': clk.summary()}
+            'roofline': roofline, 'roofline_materialized': roof_mat, 'roofline_onthefly': roof_tc,
+            'form': 'onthefly' if form == _native.FORM_ONTHEFLY else 'materialized',
+            'gpu_launches': int(launches), 'clocks': clk.summary()}
 
     if rank == 0 and not args.no_cpu:
         rng = np.random.default_rng(0)
@@ -300,7 +323,7 @@ def main():
         scale = (I_FULL * J_FULL) / (SAMPLE[0] * SAMPLE[1])
         it_gpu = iters / args.steps
         cpu_value = 1.0 / (t_cpu * scale * (it_gpu / it_cpu))
-        res_s = D.solve(D.default_cost(a_s.astype(np.float32), b_s.astype(np.float32)), G_s, CFG, 0)
+        res_s = D.solve(D.default_cost(a_s.astype(np.float32), b_s.astype(np.float32)), G_s, CFG, 0, form=args.form)
         T_gpu = res_s.tmap.cpu().numpy()
         line['parity_sample'] = {'shape': list(SAMPLE), 'coupling_max_rel_err':
                                  float(np.abs(T_gpu - T_cpu).max() / np.abs(T_cpu).max()),
@@ -313,7 +336,7 @@ def main():
     if not args.no_e2e:
         ids = np.array(['c%d' % i for i in range(len(day))])
         ds = wot.Dataset(X, wot.Frame({'day': day, 'cell_growth_rate': growth}, index=ids))
-        model = wot.OTModel(ds, growth_iters=3)
+        model = wot.OTModel(ds, growth_iters=3, form=args.form)
         model.compute_transport_map(0, 1)
         torch.cuda.synchronize()
         if pg:

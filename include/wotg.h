@@ -173,6 +173,17 @@ size_t wotg_lse_matvec_workspace_bytes(int64_t I, int64_t J, int64_t ldc);
 int wotg_lse_matvec(const float* C, int64_t I, int64_t J, int64_t ldc, const float* w, float kappa2,
                     int32_t axis, double* L, void* workspace, size_t workspace_bytes, void* stream);
 
+/* The same half-step from points, on the tensor cores (the on-the-fly form):
+ *   L[i] = log sum_j exp(w[j] - scale |x_i - y_j|^2)
+ * with X (I x d), Y (J x d) FP32 device points (row strides ldx, ldy; d <= 62),
+ * w and L FP64 device vectors, scale > 0 (the reference's cost_scale / eps).
+ * The K.dot(b * dy) of wot/ot/optimal_transport.py:133 in the log domain, with
+ * the cost of ot_model.py:249-252 recomputed tile by tile instead of stored. */
+size_t wotg_lse_points_workspace_bytes(int64_t I, int64_t J, int32_t d);
+int wotg_lse_points(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy, int32_t d,
+                    double scale, const double* w, double* L, void* workspace, size_t workspace_bytes,
+                    void* stream);
+
 /* Diagnostics (no counterpart in the reference): one 128 x 128 x 32 tensor-core
  * product D = A B^T through the FP16 split used by the on-the-fly form
  * (terms = 1: hi.hi; 3: hi.hi + hi.lo + lo.hi), with the shared-memory

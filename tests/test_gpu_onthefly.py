@@ -88,3 +88,19 @@ def test_onthefly_vs_oracle_c0_shape(eps):
     T = res.tmap.cpu().numpy()
     assert err(T, ref) <= COUPLING_TOL, err(T, ref)
     assert abs(res.stats['iterations'] - st['iterations']) <= 10
+
+
+@pytest.mark.parametrize('I,J,d', [(37, 53, 30), (300, 1000, 30), (129, 257, 50)])
+def test_lse_points_primitive(I, J, d):
+    """wotg_lse_points against an FP64 log-sum-exp of the same points."""
+    from wot_gb300.ot import device as D
+    x, y, _ = _points(I, J, d, 3)
+    rng = np.random.default_rng(4)
+    w = rng.normal(size=J) * 3
+    C = ((x.astype(np.float64)[:, None, :] - y.astype(np.float64)[None, :, :]) ** 2).sum(-1)
+    scale = 1.0 / (np.median(C) * 0.05)
+    L = D.lse_points(x, y, w, scale).cpu().numpy()
+    z = w[None, :] - scale * C
+    m = z.max(axis=1)
+    ref = m + np.log(np.exp(z - m[:, None]).sum(axis=1))
+    np.testing.assert_allclose(L, ref, rtol=0, atol=5e-5 * max(1.0, np.abs(ref).max()))

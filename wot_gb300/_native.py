@@ -34,6 +34,7 @@ EXPORTS = (
     'wotg_compute_transport_matrix', 'wotg_apply_coupling_f64', 'wotg_launch_count',
     'wotg_lse_matvec_workspace_bytes', 'wotg_lse_matvec', 'wotg_noalloc_scratch_bytes',
     'wotg_compute_transport_matrix_noalloc', 'wotg_problem_workspace_bytes', 'wotg_tc_selftest',
+    'wotg_lse_points_workspace_bytes', 'wotg_lse_points',
 )
 
 
@@ -89,6 +90,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         'wotg_solve_workspace_bytes': (ctypes.c_size_t, [i64, i64, i64]),
         'wotg_problem_workspace_bytes': (ctypes.c_size_t, [ctypes.POINTER(Problem)]),
         'wotg_tc_selftest': (ctypes.c_int, [vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, i32, vp, vp]),
+        'wotg_lse_points_workspace_bytes': (ctypes.c_size_t, [i64, i64, i32]),
+        'wotg_lse_points': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, vp, vp, vp, ctypes.c_size_t, vp]),
         'wotg_compute_transport_matrix': (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params),
                                                          vp, vp, vp, vp, vp, ctypes.POINTER(Stats),
                                                          vp, ctypes.c_size_t, vp]),

@@ -6,6 +6,7 @@
 // dimensions, runs here as an FP16 split-precision MMA (x = hi + lo, three
 // products hi.hi + hi.lo + lo.hi, FP32 accumulation in TMEM).
 #include <algorithm>
+#include <cmath>
 
 #include "wotg_common.cuh"
 #include "wotg_onthefly.cuh"
@@ -133,7 +134,7 @@ __global__ void tc_pack_kernel(const float* __restrict__ X, int64_t n, int64_t l
 }
 
 // Column-form bias columns of every point (and of the padding points):
-//   bias_q = (pot_q / eps + lsc_q) log2 e - kappa2 |q|^2
+//   bias_q = (pot_q / eps + lsc_q) log2 e - kappa2 |q|^2      (lsc may be null: 0)
 // (-inf -> a large negative finite value, i.e. weight 0; NaN / +inf -> NaN so
 // that non-finite potentials propagate like in the materialised form).
 __global__ void tc_bias_pack_kernel(int64_t n, int64_t n_pad, const double* __restrict__ pot,
@@ -143,7 +144,7 @@ __global__ void tc_bias_pack_kernel(int64_t n, int64_t n_pad, const double* __re
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += (int64_t)gridDim.x * blockDim.x) {
     __half h1, l1, h2, l2;
     const __half zero = __float2half_rn(0.f);
-    double beta = i < n ? (pot[i] * inv_eps + lsc[i]) * kLog2e - kappa2d * norm[i] : -INFINITY;
+    double beta = i < n ? (pot[i] * inv_eps + (lsc ? lsc[i] : 0.0)) * kLog2e - kappa2d * norm[i] : -INFINITY;
     if (beta != beta || beta == INFINITY) {
       h1 = __float2half_rn(NAN);
       l1 = h2 = l2 = zero;
@@ -488,6 +489,49 @@ int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int 
   return WOTG_OK;
 }
 
+
+// Finish of the standalone half-step: L_i = ln2 (m + log2 s) - scale |x_i|^2.
+__global__ void lse_points_finish_kernel(int64_t n, int nq, int ctas, int nparts, const float2* __restrict__ part,
+                                         const double* __restrict__ norm, double scale, double* __restrict__ L) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t t = i >> 7;
+  const int64_t total = ((n + 127) >> 7) * (int64_t)nq;
+  const int64_t c_lo = tc_cta_of(t * nq, total, ctas);
+  const int64_t c_hi = tc_cta_of((t + 1) * nq - 1, total, ctas);
+  float m = kNegBig, s = 0.f;
+  for (int64_t cc = c_lo; cc <= c_hi; ++cc) {
+    const float2* pp = part + ((cc + t) * 128 + (i & 127)) * nparts;
+    for (int k = 0; k < nparts; ++k) lse_merge(m, s, pp[k].x, pp[k].y);
+  }
+  L[i] = ((double)m + log2((double)s)) * kLn2 - scale * norm[i];
+}
+
+struct PointsLayout {
+  int kp, n_xt, n_yt, ctas;
+  __half* Xa;
+  __half* Yb;
+  double* normX;
+  double* normY;
+  float2* part;
+  int* err;
+};
+
+static size_t points_layout(Bump& b, int64_t I, int64_t J, int d, PointsLayout& P) {
+  P.kp = tc_kp(d);
+  P.n_xt = (int)((I + 127) / 128);
+  P.n_yt = (int)((J + 127) / 128);
+  P.ctas = (int)std::min<int64_t>((int64_t)sm_count() * tc_ctas_per_sm(P.kp), (int64_t)P.n_xt * P.n_yt);
+  const size_t tb = tc_tile_bytes(P.kp);
+  P.Xa = reinterpret_cast<__half*>(b.take<unsigned char>(tb * P.n_xt));
+  P.Yb = reinterpret_cast<__half*>(b.take<unsigned char>(tb * P.n_yt));
+  P.normX = b.take<double>(I);
+  P.normY = b.take<double>(J);
+  P.part = b.take<float2>((size_t)(P.ctas + P.n_xt) * 128 * kTcParts);
+  P.err = b.take<int>(4);
+  return b.off + 256;
+}
+
 }  // namespace wotg
 
 using namespace wotg;
@@ -497,6 +541,40 @@ extern "C" int wotg_tc_selftest(const float* A, const float* B, float* D, uint32
   if (!A || !B || !D || !err || lbo > 512 || sbo > 512 || (lbo & 15) || (sbo & 15) || (terms != 1 && terms != 3))
     return WOTG_BADARG;
   tc_selftest_kernel<<<1, 128, 0, (cudaStream_t)stream>>>(A, B, D, lbo, sbo, terms, err);
+  WOTG_LAUNCHED();
+  return WOTG_OK;
+}
+
+extern "C" size_t wotg_lse_points_workspace_bytes(int64_t I, int64_t J, int32_t d) {
+  if (I <= 0 || J <= 0 || d < 1 || d > tc_max_dim()) return 0;
+  Bump b{nullptr, 0};
+  PointsLayout P{};
+  return points_layout(b, I, J, d, P);
+}
+
+extern "C" int wotg_lse_points(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy,
+                               int32_t d, double scale, const double* w, double* L, void* workspace,
+                               size_t workspace_bytes, void* stream) {
+  if (!X || !Y || !w || !L || I <= 0 || J <= 0 || d < 1 || d > tc_max_dim() || ldx < d || ldy < d ||
+      !(scale > 0))
+    return WOTG_BADARG;
+  if (!workspace || workspace_bytes < wotg_lse_points_workspace_bytes(I, J, d)) return WOTG_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  Bump b{reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255)), 0};
+  PointsLayout P{};
+  points_layout(b, I, J, d, P);
+  const double sigma = std::sqrt(scale);
+  WOTG_CUDA(cudaMemsetAsync(P.err, 0, sizeof(int), st));
+  int s = tc_pack_points(X, I, ldx, d, P.kp, (float)(2.0 * kLog2e * sigma), 1, P.Xa, P.normX, st);
+  if (s) return s;
+  s = tc_pack_points(Y, J, ldy, d, P.kp, (float)sigma, 0, P.Yb, P.normY, st);
+  if (s) return s;
+  s = tc_pack_bias(J, w, nullptr, P.normY, 1.0, scale * kLog2e, d, P.kp, P.Yb, st);
+  if (s) return s;
+  s = tc_lse_launch(P.Xa, P.n_xt, P.Yb, P.n_yt, P.kp, P.ctas, P.part, P.err, st);
+  if (s) return s;
+  lse_points_finish_kernel<<<(unsigned)((I + 255) / 256), 256, 0, st>>>(I, P.n_yt, P.ctas, kTcParts, P.part,
+                                                                        P.normX, scale, L);
   WOTG_LAUNCHED();
   return WOTG_OK;
 }

@@ -205,3 +205,22 @@ def apply_coupling(X, P, transpose: bool, normalize: bool):
                                              int(normalize), out.data_ptr(), _stream()),
             'wotg_apply_coupling_f64')
     return out
+
+
+def lse_points(x, y, w, scale: float):
+    """L_i = log sum_j exp(w_j - scale |x_i - y_j|^2) on the tensor cores (FP64 out)."""
+    torch = _torch()
+    X = _dev_f32(x, torch)
+    Y = _dev_f32(y, torch)
+    W = _dev_f64(w, torch).reshape(-1)
+    I, d = X.shape
+    J = Y.shape[0]
+    lib = N.load()
+    nbytes = lib.wotg_lse_points_workspace_bytes(I, J, d)
+    if nbytes == 0:
+        raise ValueError('invalid points for the on-the-fly half-step (d <= 62)')
+    ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
+    L = torch.empty(I, dtype=torch.float64, device='cuda')
+    N.check(lib.wotg_lse_points(X.data_ptr(), I, X.stride(0), Y.data_ptr(), J, Y.stride(0), d, float(scale),
+                                W.data_ptr(), L.data_ptr(), ws.data_ptr(), nbytes, _stream()), 'wotg_lse_points')
+    return L

@@ -38,7 +38,9 @@ class OTModel:
     **kwargs
         ``config``, ``cell_filter``, ``gene_filter``, ``cell_day_filter``,
         ``ncounts``, ``ncells``, ``solver`` ('duality_gap' | 'fixed_iters'),
-        ``parameters`` (2-column file), and any ot_config key.
+        ``parameters`` (2-column file), and any ot_config key. The GPU-only
+        ``form`` ('auto' | 'materialized' | 'onthefly') picks how the cost is
+        read by the Sinkhorn half-steps; it is not part of ot_config.
     """
 
     def __init__(self, matrix, day_field='day', covariate_field='covariate',
@@ -53,6 +55,8 @@ class OTModel:
         day_filter = kwargs.pop('cell_day_filter', None)
         ncounts = kwargs.pop('ncounts', None)
         ncells = kwargs.pop('ncells', None)
+        # GPU-only knob, kept out of ot_config: 'auto' | 'materialized' | 'onthefly'
+        self.form = kwargs.pop('form', 'auto')
         self.matrix = _filter(self.matrix, cell_filter, gene_filter)
         if day_filter is not None:
             days = [float(day) for day in day_filter.split(',')] if isinstance(day_filter, str) else day_filter
@@ -246,7 +250,7 @@ class OTModel:
             config['G'] = np.ones(n0)
         sid = ot.native_solver_id(self.solver)
         cost = C if isinstance(C, D.DeviceCost) else D.cost_from_dense(C)
-        res = D.solve(cost, config['G'], config, sid, want_tmap=True)
+        res = D.solve(cost, config['G'], config, sid, want_tmap=True, form=self.form)
         tmap = res.tmap.cpu().numpy()
         learned = [np.asarray(config['G'], dtype=np.float64)] + [g.cpu().numpy() for g in res.learned_growth[1:]]
         learned.append(res.row_sums.cpu().numpy())
