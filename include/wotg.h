@@ -200,6 +200,83 @@ int wotg_tc_selftest(const float* A, const float* B, float* D, uint32_t lbo, uin
 int wotg_apply_coupling_f64(const double* X, int64_t I, int64_t J, const double* P, int32_t k,
                             int32_t transpose, int32_t normalize, double* out, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Batched solves. The reference solves day pairs one after another
+ * (OTModel.compute_all_transport_maps, wot/ot/ot_model.py:124-201, one
+ * compute_transport_matrix per pair, ot_model.py:318) and a parameter sweep
+ * repeats that per parameter set; here every (pair, parameter set) item of a
+ * batch advances together: each Sinkhorn half-step is one persistent launch
+ * over all pairs that reads a pair's cost once for all of its active items,
+ * the reference's control flow (epsilon stages, batches, absorption, stage and
+ * duality-gap tests, growth iterations) runs per item on the device, and the
+ * iterations are replayed from a captured CUDA graph. Results per item are the
+ * reference's (duality-gap solver only), returned as potentials:
+ *   tmap_ij = exp((u_bar_i + v_bar_j - cost_scale C_ij) / eps) * scale
+ * with eps = stats.final_epsilon and scale = 1/J (or 1 when max_iter was hit).
+ * ------------------------------------------------------------------------ */
+
+/* One day pair of a batch: its FP32 cost (as in wotg_problem) and the cost's
+ * transpose, both with +INF padding, and the growth G of its source cells. */
+typedef struct wotg_pair {
+  int64_t I;
+  int64_t J;
+  const float* C;         /* device, I x ldc */
+  int64_t ldc;
+  const float* CT;        /* device, J x ldct: C transposed (wotg_transpose_cost) */
+  int64_t ldct;
+  double cost_scale;
+  const double* G;        /* device, I */
+} wotg_pair;
+
+/* One transport problem of a batch: a pair, the solver parameters (solver must
+ * be WOTG_SOLVER_DUALITY_GAP) and where its outputs go in the batch's
+ * concatenated output arrays. */
+typedef struct wotg_item {
+  int32_t pair;
+  int32_t reserved_;
+  wotg_params params;
+  int64_t row_offset;     /* first entry of this item's I-vectors in u_bar and row_sums */
+  int64_t col_offset;     /* first entry of its J-vectors in v_bar */
+  int64_t growth_offset;  /* first entry of its growth_iters x I learned growth */
+} wotg_item;
+
+/* CT (J x ldct) = C^T for the I x J valid entries of C, +INF in columns
+ * [I, ldct). ldct >= I, ldct % 4 == 0. Building block of a batch (no
+ * counterpart in the reference). */
+int wotg_transpose_cost(const float* C, int64_t I, int64_t J, int64_t ldc, float* CT, int64_t ldct, void* stream);
+
+/* Solves every item of the batch (see above). Outputs (device): u_bar, v_bar,
+ * row_sums (tmap.sum(axis=1), the reference's learned growth appended by
+ * OTModel, ot_model.py:319) at each item's offsets; learned_growth may be NULL.
+ * stats and statuses (wotg_status per item) are HOST arrays of n_items, either
+ * may be NULL. Returns WOTG_OK unless a call failed; per-item outcomes
+ * (WOTG_MAX_ITER, WOTG_NONFINITE) are in statuses. The iterations run on an
+ * internal stream ordered after `stream`; the call returns when all are done. */
+size_t wotg_batch_workspace_bytes(const wotg_pair* pairs, int32_t n_pairs, const wotg_item* items, int32_t n_items);
+int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const wotg_item* items, int32_t n_items,
+                       double* u_bar, double* v_bar, double* row_sums, double* learned_growth, wotg_stats* stats,
+                       int32_t* statuses, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Multi right-hand-side half-step on one materialised cost (row form of
+ * wotg_lse_matvec for K weight vectors at once; each cost element is read once):
+ *   L[k * ldl + i] = ln2 * log2 sum_j 2^(W[k * ldw + j] - kappa2[k] C_ij),  k < K
+ * W: K rows of ldw >= roundup(J, 4) floats (16-byte aligned), finite or -INF;
+ * kappa2: HOST array of K positive values. The K.dot(b * dy) of
+ * optimal_transport.py:133 for several b, and the pull-back p @ tmap.T of
+ * transport_map_model.py:356 for several populations on a coupling held as
+ * potentials. */
+size_t wotg_lse_matvec_multi_workspace_bytes(int64_t I, int32_t K);
+int wotg_lse_matvec_multi(const float* C, int64_t I, int64_t J, int64_t ldc, const float* W, int64_t ldw,
+                          const float* kappa2, int32_t K, double* L, int64_t ldl, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
+/* Dense FP64 coupling from potentials (a batch item's map, or any solve's):
+ *   out[i * J + j] = exp((u_bar_i + v_bar_j - cost_scale C_ij) / eps + log_scale)
+ * (log_scale = -log J for the reference's return value R / J). */
+int wotg_coupling_from_potentials(const float* C, int64_t I, int64_t J, int64_t ldc, double cost_scale, double eps,
+                                  const double* u_bar, const double* v_bar, double log_scale, double* out,
+                                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,7 +34,9 @@ EXPORTS = (
     'wotg_compute_transport_matrix', 'wotg_apply_coupling_f64', 'wotg_launch_count',
     'wotg_lse_matvec_workspace_bytes', 'wotg_lse_matvec', 'wotg_noalloc_scratch_bytes',
     'wotg_compute_transport_matrix_noalloc', 'wotg_problem_workspace_bytes', 'wotg_tc_selftest',
-    'wotg_lse_points_workspace_bytes', 'wotg_lse_points',
+    'wotg_lse_points_workspace_bytes', 'wotg_lse_points', 'wotg_transpose_cost', 'wotg_batch_workspace_bytes',
+    'wotg_solve_batched', 'wotg_lse_matvec_multi_workspace_bytes', 'wotg_lse_matvec_multi',
+    'wotg_coupling_from_potentials',
 )
 
 
@@ -64,6 +66,17 @@ class Problem(ctypes.Structure):
                 ('cost_scale', ctypes.c_double), ('G', ctypes.c_void_p), ('X', ctypes.c_void_p),
                 ('ldx', ctypes.c_int64), ('Y', ctypes.c_void_p), ('ldy', ctypes.c_int64), ('d', ctypes.c_int32),
                 ('form', ctypes.c_int32)]
+
+
+class Pair(ctypes.Structure):
+    _fields_ = [('I', ctypes.c_int64), ('J', ctypes.c_int64), ('C', ctypes.c_void_p), ('ldc', ctypes.c_int64),
+                ('CT', ctypes.c_void_p), ('ldct', ctypes.c_int64), ('cost_scale', ctypes.c_double),
+                ('G', ctypes.c_void_p)]
+
+
+class Item(ctypes.Structure):
+    _fields_ = [('pair', ctypes.c_int32), ('reserved_', ctypes.c_int32), ('params', Params),
+                ('row_offset', ctypes.c_int64), ('col_offset', ctypes.c_int64), ('growth_offset', ctypes.c_int64)]
 
 
 _lib = None
@@ -100,6 +113,14 @@ def load(path: str | None = None) -> ctypes.CDLL:
         'wotg_noalloc_scratch_bytes': (ctypes.c_size_t, []),
         'wotg_compute_transport_matrix_noalloc': (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params),
                                                                  vp, vp, vp, vp, vp, ctypes.POINTER(Stats), vp]),
+        'wotg_transpose_cost': (ctypes.c_int, [vp, i64, i64, i64, vp, i64, vp]),
+        'wotg_batch_workspace_bytes': (ctypes.c_size_t, [ctypes.POINTER(Pair), i32, ctypes.POINTER(Item), i32]),
+        'wotg_solve_batched': (ctypes.c_int, [ctypes.POINTER(Pair), i32, ctypes.POINTER(Item), i32, vp, vp, vp, vp,
+                                              ctypes.POINTER(Stats), ctypes.POINTER(i32), vp, ctypes.c_size_t, vp]),
+        'wotg_lse_matvec_multi_workspace_bytes': (ctypes.c_size_t, [i64, i32]),
+        'wotg_lse_matvec_multi': (ctypes.c_int, [vp, i64, i64, i64, vp, i64, ctypes.POINTER(ctypes.c_float), i32,
+                                                 vp, i64, vp, ctypes.c_size_t, vp]),
+        'wotg_coupling_from_potentials': (ctypes.c_int, [vp, i64, i64, i64, dbl, dbl, vp, vp, dbl, vp, vp]),
         'wotg_lse_matvec_workspace_bytes': (ctypes.c_size_t, [i64, i64, i64]),
         'wotg_lse_matvec': (ctypes.c_int, [vp, i64, i64, i64, vp, ctypes.c_float, i32, vp, vp, ctypes.c_size_t,
                                            vp]),

@@ -1,0 +1,43 @@
+// wotg_coef.cuh — per-epsilon coefficients of the Sinkhorn updates, shared by
+// the single-problem driver (host) and the batched driver (device).
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+namespace wotg {
+
+struct Coef {
+  double eps, inv_eps;
+  double alpha1, alpha2;
+  double inv_l1e, inv_l2e;  // 1/(lambda + eps)
+  double lambda1, lambda2;
+  double logI, logJ, logq, q;
+  double kappa;             // cost_scale / eps
+  float kappa2;             // cost_scale / eps * log2(e)
+};
+
+// The reference's exponents alpha1 = lambda1 / (lambda1 + eps) and
+// alpha2 = lambda2 / (lambda2 + eps) (optimal_transport.py:119-121 / :201-203)
+// and the constants the log-domain updates need.
+__host__ __device__ inline Coef make_coef(double eps, double lambda1, double lambda2, double cost_scale, int64_t I,
+                                          int64_t J, double q) {
+  Coef c;
+  c.eps = eps;
+  c.inv_eps = 1.0 / eps;
+  c.alpha1 = lambda1 / (lambda1 + eps);
+  c.alpha2 = lambda2 / (lambda2 + eps);
+  c.inv_l1e = 1.0 / (lambda1 + eps);
+  c.inv_l2e = 1.0 / (lambda2 + eps);
+  c.lambda1 = lambda1;
+  c.lambda2 = lambda2;
+  c.logI = log((double)I);
+  c.logJ = log((double)J);
+  c.q = q;
+  c.logq = log(q);
+  c.kappa = cost_scale / eps;
+  c.kappa2 = (float)(cost_scale / eps * 1.4426950408889634074);
+  return c;
+}
+
+}  // namespace wotg

@@ -31,6 +31,7 @@
 #include <cstdio>
 #include <cstring>
 
+#include "wotg_coef.cuh"
 #include "wotg_common.cuh"
 #include "wotg_onthefly.cuh"
 
@@ -60,15 +61,6 @@ struct Vecs {
 constexpr int kNq = 8;
 constexpr int kRedBlocks = 296;
 
-struct Coef {
-  double eps, inv_eps;
-  double alpha1, alpha2;
-  double inv_l1e, inv_l2e;  // 1/(lambda + eps)
-  double lambda1, lambda2;
-  double logI, logJ, logq, q;
-  double kappa;             // cost_scale / eps
-  float kappa2;             // cost_scale / eps * log2(e)
-};
 
 // Buffers of the on-the-fly (tensor-core) form.
 struct TcState {
@@ -566,22 +558,7 @@ struct Solver {
   TcState tc;
 
   Coef coef(double eps, const wotg_params& P, double q) const {
-    Coef c;
-    c.eps = eps;
-    c.inv_eps = 1.0 / eps;
-    c.alpha1 = P.lambda1 / (P.lambda1 + eps);
-    c.alpha2 = P.lambda2 / (P.lambda2 + eps);
-    c.inv_l1e = 1.0 / (P.lambda1 + eps);
-    c.inv_l2e = 1.0 / (P.lambda2 + eps);
-    c.lambda1 = P.lambda1;
-    c.lambda2 = P.lambda2;
-    c.logI = std::log((double)g.I);
-    c.logJ = std::log((double)g.J);
-    c.q = q;
-    c.logq = std::log(q);
-    c.kappa = cost_scale / eps;
-    c.kappa2 = (float)(cost_scale / eps * kLog2e);
-    return c;
+    return make_coef(eps, P.lambda1, P.lambda2, cost_scale, g.I, g.J, q);
   }
 
   int vec_blocks(int64_t n) const { return (int)std::max<int64_t>(1, (n + 255) / 256); }

@@ -224,3 +224,39 @@ def lse_points(x, y, w, scale: float):
     N.check(lib.wotg_lse_points(X.data_ptr(), I, X.stride(0), Y.data_ptr(), J, Y.stride(0), d, float(scale),
                                 W.data_ptr(), L.data_ptr(), ws.data_ptr(), nbytes, _stream()), 'wotg_lse_points')
     return L
+
+
+def transpose_cost(cost: DeviceCost):
+    """C^T (J x ldct FP32, +inf padding) of a device cost; the column form a batch reads."""
+    torch = _torch()
+    ldct = N.round_up(cost.I, 4)
+    CT = torch.empty((cost.J, ldct), dtype=torch.float32, device='cuda')
+    N.check(N.load().wotg_transpose_cost(cost.C.data_ptr(), cost.I, cost.J, cost.ldc, CT.data_ptr(), ldct,
+                                         _stream()), 'wotg_transpose_cost')
+    return CT
+
+
+def lse_multi(C, I: int, J: int, ldc: int, W, kappa2):
+    """L[k, i] = log sum_j exp2(W[k, j] - kappa2[k] C[i, j]) for K weight rows at once
+    (one read of C); W is K x ldw FP32 on the device (ldw >= roundup(J, 4))."""
+    torch = _torch()
+    lib = N.load()
+    K, ldw = W.shape
+    k2 = (ctypes.c_float * K)(*[float(x) for x in kappa2])
+    nbytes = lib.wotg_lse_matvec_multi_workspace_bytes(I, K)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
+    L = torch.empty((K, I), dtype=torch.float64, device='cuda')
+    N.check(lib.wotg_lse_matvec_multi(C.data_ptr(), I, J, ldc, W.data_ptr(), ldw, k2, K, L.data_ptr(), I,
+                                      ws.data_ptr(), nbytes, _stream()), 'wotg_lse_matvec_multi')
+    return L
+
+
+def coupling_from_potentials(cost: DeviceCost, u_bar, v_bar, eps: float, log_scale: float):
+    """Dense FP64 coupling exp((u_bar_i + v_bar_j - scale C_ij) / eps + log_scale)."""
+    torch = _torch()
+    out = torch.empty((cost.I, cost.J), dtype=torch.float64, device='cuda')
+    N.check(N.load().wotg_coupling_from_potentials(cost.C.data_ptr(), cost.I, cost.J, cost.ldc, float(cost.scale),
+                                                   float(eps), u_bar.data_ptr(), v_bar.data_ptr(),
+                                                   float(log_scale), out.data_ptr(), _stream()),
+            'wotg_coupling_from_potentials')
+    return out
