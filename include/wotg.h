@@ -260,7 +260,8 @@ int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const wotg_item*
 /* Multi right-hand-side half-step on one materialised cost (row form of
  * wotg_lse_matvec for K weight vectors at once; each cost element is read once):
  *   L[k * ldl + i] = ln2 * log2 sum_j 2^(W[k * ldw + j] - kappa2[k] C_ij),  k < K
- * W: K rows of ldw >= roundup(J, 4) floats (16-byte aligned), finite or -INF;
+ * W: K rows of ldw >= roundup(J, 4) floats (16-byte aligned), finite or -INF
+ * (entries [J, ldw) finite: they meet the cost's +INF padding);
  * kappa2: HOST array of K positive values. The K.dot(b * dy) of
  * optimal_transport.py:133 for several b, and the pull-back p @ tmap.T of
  * transport_map_model.py:356 for several populations on a coupling held as

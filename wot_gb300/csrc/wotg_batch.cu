@@ -19,11 +19,14 @@
 //    half-steps, `item_kernel` applies tau-absorption and counts iterations and
 //    batches; a check pass recomputes the row sums of items whose batch ended
 //    in the final stage (and sum exp(-C/eps) for items entering it);
-//    `test_kernel` evaluates the stage-exit test or the duality gap and moves
-//    each item on (next batch, next stage, next growth iteration, done). The
-//    last CTA of each of those kernels rebuilds the per-pair lists of items the
-//    next pass will see.
-//  * Five launches per iteration of the whole batch, captured B iterations at a
+//    `test_kernel` evaluates the stage-exit test or the duality gap and decides
+//    each item's next step (next batch, next stage, next growth iteration,
+//    done), whose O(I + J) work `apply_kernel` does. Each item's O(I + J) loops
+//    are split over several CTAs (FP64 is 1/64 of the FP32 rate on this part,
+//    so one CTA per item would serialise them), with fixed-order sums. The last
+//    CTA of each of those kernels rebuilds the per-pair lists of items the next
+//    pass will see.
+//  * Six launches per iteration of the whole batch, captured B iterations at a
 //    time in a CUDA graph and replayed until no item is active.
 //
 // Item state and iteration counts follow the single-problem driver
@@ -92,8 +95,15 @@ struct Item {
   Coef c;
   double scale_factor, eps_i, gap, sumK, threshold, q;
   long long it, it_total, checks, absorptions;
-  int status, stage, batch_cnt, parity, skip_row, due, need_sumk, gi, hit_max_iter, pad1;
+  int status, stage, batch_cnt, parity, skip_row, due, need_sumk, gi, hit_max_iter, action;
+  int first_blk, nblk;  // this item's CTAs in the per-item kernels
+  double eps_prev, q_next;
   unsigned long long maxslot[2];
+};
+
+// CTA b of a per-item kernel works on item blk[b].item, slice blk[b].rank.
+struct ItemBlock {
+  int item, rank;
 };
 
 struct PassArgs {
@@ -119,10 +129,15 @@ struct BatchArgs {
   Entry* col_list;
   int* chk_n;
   Entry* chk_list;            // capacity 2 K_p per pair at 2 pair_off[p]
-  int* counters;              // [0] row ticket, [1] col ticket, [2] check ticket, [3..5] last-block counters
+  int* counters;              // [0] row, [1] col, [2] check tickets; [3..7] grid-wide last-block counters
   int* active;
   const float* zeros;
+  const ItemBlock* blk;       // per-item kernels: one entry per CTA
+  int* item_ctr;              // per item: CTAs of the current per-item kernel that finished
+  double* part;               // per CTA: kNq partial sums
 };
+
+constexpr int kNq = 10;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -132,6 +147,33 @@ __device__ __forceinline__ void cp_async16(uint32_t saddr, const void* g, uint32
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Packed FP32 pairs (sm_100 family): one instruction for two elements.
+__device__ __forceinline__ uint64_t pk(float x, float y) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+  return r;
+}
+__device__ __forceinline__ float2 upk(uint64_t r) {
+  float2 v;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+  return v;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// 2^(t - o) for a packed pair t and packed offset (-o, -o).
+__device__ __forceinline__ uint64_t ex2_off(uint64_t t, uint64_t mo) {
+  const float2 v = upk(add2(t, mo));
+  return pk(ex2(v.x), ex2(v.y));
+}
 
 __device__ __forceinline__ float warp_sumf(float x) {
 #pragma unroll
@@ -143,6 +185,7 @@ __device__ __forceinline__ float warp_sumf(float x) {
 // Per-(row, item) epilogues: the single-problem driver's a- and b-updates
 // (optimal_transport.py:131-135) on the item's vectors.
 // ---------------------------------------------------------------------------
+// Both return the new log-scaling (the absorption test takes exp of its maximum).
 __device__ __forceinline__ double item_a_update(Item& it, int64_t i, double L) {
   const Coef& c = it.c;
   const double ui = it.u[i];
@@ -151,7 +194,7 @@ __device__ __forceinline__ double item_a_update(Item& it, int64_t i, double L) {
   it.la_old[i] = it.la[i];
   it.la[i] = la_new;
   it.wrow[i] = (float)((ui * c.inv_eps + la_new) * kLog2e);
-  return exp(la_new);
+  return la_new;
 }
 
 __device__ __forceinline__ double item_b_update(Item& it, int64_t j, double L) {
@@ -162,27 +205,36 @@ __device__ __forceinline__ double item_b_update(Item& it, int64_t j, double L) {
   it.lb_old[j] = it.lb[j];
   it.lb[j] = lb_new;
   it.wcol[j] = (float)((vj * c.inv_eps + lb_new) * kLog2e);
-  return exp(lb_new);
+  return lb_new;
 }
 
-// L2 = base-2 log-sum-exp of row r for entry e; returns the value whose
-// maximum over rows feeds the absorption test (a_i or b_j), else 0.
+// L2 = o + log2(s) for a sum s = m 2^e: the exponent exactly, the FP32 log2 of
+// the mantissa (absolute error ~1e-7, below the FP32 sum's own rounding), no
+// FP64 transcendental.
+__device__ __forceinline__ double lse2(float o, float s) {
+  int e;
+  const float m = frexpf(s, &e);
+  return (double)o + (double)e + (double)log2f(m);
+}
+
+// L2 = base-2 log-sum-exp of row r for entry e; returns the log-scaling whose
+// maximum over rows feeds the absorption test (log a_i or log b_j), else -inf.
 __device__ __forceinline__ double entry_epilogue(Item* items, const Entry& e, int64_t r, double L2) {
   const double L = L2 * kLn2;
   switch (e.mode) {
     case kOut:
       e.out[r] = L;
       if (e.o) e.o[r] = (float)L2;
-      return 0.0;
+      return -INFINITY;
     case kFresh: {
       Item& it = items[e.item];
       it.Lrow[r] = L;
       it.orow[r] = (float)L2;
-      return 0.0;
+      return -INFINITY;
     }
     case kSumK:
       items[e.item].rsum[r] = exp(L);
-      return 0.0;
+      return -INFINITY;
     case kRowA: {
       Item& it = items[e.item];
       it.Lrow[r] = L;
@@ -196,7 +248,7 @@ __device__ __forceinline__ double entry_epilogue(Item* items, const Entry& e, in
       return item_b_update(it, r, L);
     }
     default:
-      return 0.0;
+      return -INFINITY;
   }
 }
 
@@ -291,6 +343,29 @@ __device__ __forceinline__ void run_group(const PassArgs& A, const Seg& sg, int 
       if (ch + 1 < nch) nxt[rr] = load_cost(crow[rr], (int64_t)(ch + 1) * 32 + lane, nv, valid[rr]);
     }
     const float* wb = &sW[ch & 1][0][lane * 4];
+    if (SPEC) {
+      uint64_t c01[RW], c23[RW];
+#pragma unroll
+      for (int rr = 0; rr < RW; ++rr) {
+        c01[rr] = pk(cc[rr].x, cc[rr].y);
+        c23[rr] = pk(cc[rr].z, cc[rr].w);
+      }
+#pragma unroll
+      for (int k = 0; k < KG; ++k) {
+        if (k < ng) {
+          const float4 w = *reinterpret_cast<const float4*>(wb + k * kChunk);
+          const uint64_t w01 = pk(w.x, w.y), w23 = pk(w.z, w.w), kk = pk(nk2[k], nk2[k]);
+#pragma unroll
+          for (int rr = 0; rr < RW; ++rr) {
+            const uint64_t mo = pk(-off[rr][k], -off[rr][k]);
+            const uint64_t e01 = ex2_off(fma2(kk, c01[rr], w01), mo);
+            const uint64_t e23 = ex2_off(fma2(kk, c23[rr], w23), mo);
+            const float2 e = upk(add2(e01, e23));
+            acc[rr][k] += e.x + e.y;
+          }
+        }
+      }
+    } else {
 #pragma unroll
     for (int k = 0; k < KG; ++k) {
       if (k < ng) {
@@ -301,10 +376,7 @@ __device__ __forceinline__ void run_group(const PassArgs& A, const Seg& sg, int 
           const float t1 = fmaf(nk2[k], cc[rr].y, w.y);
           const float t2 = fmaf(nk2[k], cc[rr].z, w.z);
           const float t3 = fmaf(nk2[k], cc[rr].w, w.w);
-          if (SPEC) {
-            const float o = off[rr][k];
-            acc[rr][k] += (ex2(t0 - o) + ex2(t1 - o)) + (ex2(t2 - o) + ex2(t3 - o));
-          } else {
+          {
             const float m = off[rr][k];
             const float mn = fmaxf(m, fmaxf(fmaxf(t0, t1), fmaxf(t2, t3)));
             acc[rr][k] = acc[rr][k] * ex2(m - mn) + ((ex2(t0 - mn) + ex2(t1 - mn)) + (ex2(t2 - mn) + ex2(t3 - mn)));
@@ -312,6 +384,7 @@ __device__ __forceinline__ void run_group(const PassArgs& A, const Seg& sg, int 
           }
         }
       }
+    }
     }
     __syncthreads();
   }
@@ -328,7 +401,7 @@ __device__ __forceinline__ void run_group(const PassArgs& A, const Seg& sg, int 
       }
     }
   // Lane k finishes entry k.
-  double vmax = 0.0;
+  double vmax = -INFINITY;
 #pragma unroll
   for (int rr = 0; rr < RW; ++rr) {
     float s = 0.f, o = 0.f;
@@ -353,11 +426,64 @@ __device__ __forceinline__ void run_group(const PassArgs& A, const Seg& sg, int 
       }
     }
     if (mine) {
-      const double L2 = (double)o + log2((double)s);
-      vmax = fmax(vmax, entry_epilogue(A.items, gp[lane], row[rr], L2));
+      vmax = fmax(vmax, entry_epilogue(A.items, gp[lane], row[rr], lse2(o, s)));
     }
   }
   if (lane < KG) s_vmax[warp][lane] = vmax;
+}
+
+// One entry over the tile's rows (a pair with a single active item, as in the
+// tail of a batch): each warp streams its rows with 128-bit loads of the cost
+// and the weights (L1/L2-resident), no shared-memory staging and no barrier.
+// Columns past `cols` in the last float4 meet the cost's +inf padding.
+template <int RW, int KG>
+__device__ __forceinline__ void run_single(const PassArgs& A, const Seg& sg, int row0, const Entry* gp,
+                                           double (*s_vmax)[KG], int warp, int lane) {
+  const Entry e = gp[0];
+  const float nk2 = e.nk2;
+  const float4* __restrict__ w4 = reinterpret_cast<const float4*>(e.w);
+  const int64_t nq = ((int64_t)sg.cols + 3) >> 2;
+  double vmax = -INFINITY;
+#pragma unroll 1
+  for (int rr = 0; rr < RW; ++rr) {
+    const int64_t row = (int64_t)row0 + warp * RW + rr;
+    if (row >= sg.rows) break;
+    const float4* __restrict__ crow = reinterpret_cast<const float4*>(sg.C + row * sg.ldc);
+    const float o = e.o ? e.o[row] : 0.f;
+    const uint64_t kk = pk(nk2, nk2), mo = pk(-o, -o);
+    float s0 = 0.f, s1 = 0.f;
+    int64_t q = lane;
+    for (; q + 96 < nq; q += 128) {
+      float4 cc[4], ww[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) cc[t] = ld_stream(crow + q + 32 * t);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) ww[t] = __ldg(w4 + q + 32 * t);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const uint64_t e01 = ex2_off(fma2(kk, pk(cc[t].x, cc[t].y), pk(ww[t].x, ww[t].y)), mo);
+        const uint64_t e23 = ex2_off(fma2(kk, pk(cc[t].z, cc[t].w), pk(ww[t].z, ww[t].w)), mo);
+        const float2 e = upk(add2(e01, e23));
+        s0 += e.x;
+        s1 += e.y;
+      }
+    }
+    for (; q < nq; q += 32) {
+      const float4 cc = ld_stream(crow + q);
+      const float4 ww = __ldg(w4 + q);
+      s0 += ex2(fmaf(nk2, cc.x, ww.x) - o) + ex2(fmaf(nk2, cc.y, ww.y) - o);
+      s1 += ex2(fmaf(nk2, cc.z, ww.z) - o) + ex2(fmaf(nk2, cc.w, ww.w) - o);
+    }
+    float s = warp_sumf(s0 + s1);
+    float oo = o;
+    if (!(s >= kSpecLo && s <= kSpecHi)) {
+      const float2 ms = exact_row(sg.C + row * sg.ldc, sg.ldc, e.w, nk2, sg.cols, lane);
+      oo = ms.x;
+      s = ms.y;
+    }
+    if (lane == 0) vmax = fmax(vmax, entry_epilogue(A.items, e, row, lse2(oo, s)));
+  }
+  if (lane == 0) s_vmax[warp][0] = vmax;
 }
 
 template <int KG, int RW, bool SPEC>
@@ -381,17 +507,20 @@ __global__ void __launch_bounds__(kThreads) pass_kernel(PassArgs A) {
       const int ng = min(KG, nk - g0);
       if (threadIdx.x < ng) gp[threadIdx.x] = lst[g0 + threadIdx.x];
       __syncthreads();
-      run_group<KG, RW, SPEC>(A, sg, tile.row0, ng, gp, sW, s_vmax, warp, lane);
+      if (SPEC && ng == 1)
+        run_single<RW, KG>(A, sg, tile.row0, gp, s_vmax, warp, lane);
+      else
+        run_group<KG, RW, SPEC>(A, sg, tile.row0, ng, gp, sW, s_vmax, warp, lane);
       __syncthreads();
       // absorption maxima of this group: one atomic per item
       if (threadIdx.x < ng) {
         const Entry& e = gp[threadIdx.x];
         if (e.mode == kRowA || e.mode == kColB) {
-          double v = 0.0;
+          double v = -INFINITY;
 #pragma unroll
           for (int w = 0; w < kWarps; ++w) v = fmax(v, s_vmax[w][threadIdx.x]);
           Item& it = A.items[e.item];
-          atomic_max_nonneg(&it.maxslot[it.parity], v);
+          atomic_max_nonneg(&it.maxslot[it.parity], exp(v));
         }
       }
       __syncthreads();
@@ -400,8 +529,16 @@ __global__ void __launch_bounds__(kThreads) pass_kernel(PassArgs A) {
 }
 
 // ---------------------------------------------------------------------------
-// Per-item kernels (one CTA per item).
+// Per-item kernels. Item k owns CTAs [first_blk, first_blk + nblk) of each
+// launch; its O(I + J) loops are split over them (ITEM_LOOP), its sums are
+// per-CTA partials reduced in a fixed order by the item's last CTA, which also
+// takes the item's scalar decisions. The grid's last CTA rebuilds the lists.
 // ---------------------------------------------------------------------------
+enum Action : int { kActNone = 0, kActCont = 1, kActStage = 2, kActFinish = 3, kActFinishMax = 4 };
+
+#define ITEM_LOOP(var, n) \
+  for (int var = rank * kThreads + (int)threadIdx.x; var < (n); var += nblk * kThreads)
+
 template <int NQ>
 __device__ void block_sum(double (&acc)[NQ]) {
   __shared__ double sh[kWarps][NQ];
@@ -431,7 +568,7 @@ __device__ double block_max(double v) {
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t = 0.0;
+    double t = -INFINITY;
     for (int w = 0; w < kWarps; ++w) t = fmax(t, sh[w]);
     tot = t;
   }
@@ -441,16 +578,16 @@ __device__ double block_max(double v) {
   return v;
 }
 
-// True in every thread of the grid's last CTA to get here (all other CTAs'
-// writes are visible to it). The counter is reset for the next launch.
-__device__ bool last_block(int* done) {
+// True in every thread of the last CTA (of `expected`) to arrive at *ctr; all
+// other arrivals' writes are visible to it. The counter is reset for reuse.
+__device__ bool arrive_last(int* ctr, int expected) {
   __shared__ bool last;
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
-    const int t = atomicAdd(done, 1);
-    last = (t == (int)gridDim.x - 1);
-    if (last) *done = 0;
+    const int t = atomicAdd(ctr, 1);
+    last = (t == expected - 1);
+    if (last) *ctr = 0;
   }
   __syncthreads();
   if (last) __threadfence();
@@ -519,8 +656,29 @@ __device__ void build_check_lists(const BatchArgs& B) {
   }
 }
 
+// Active-item count for the host, tickets of the next iteration passes.
+__device__ void finish_body(const BatchArgs& B) {
+  build_iter_lists(B);
+  __shared__ int cnt[kWarps];
+  int n = 0;
+  for (int k = threadIdx.x; k < B.n_items; k += blockDim.x) {
+    const int s = __ldcg(&B.items[k].status);
+    n += (s == kActive || s == kMaxIterPending) ? 1 : 0;
+  }
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0) cnt[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < kWarps; ++w) t += cnt[w];
+    B.active[0] = t;
+    B.counters[0] = 0;
+    B.counters[1] = 0;
+  }
+}
+
 // Start of a solve (growth iteration) with p, logp, q in place: stage 0 with
-// the single-problem driver's epsilon arithmetic (eps0 * sf / sf).
+// the single-problem driver's epsilon arithmetic (eps0 * sf / sf). Scalars only.
 __device__ void start_solve(Item& it) {
   it.scale_factor = exp(-log(it.epsilon) / kScalings);
   double eps = it.epsilon0 * it.scale_factor;
@@ -538,13 +696,14 @@ __device__ void start_solve(Item& it) {
   it.threshold = kScalings == 0 ? it.tolerance : 1e-6;
   it.need_sumk = kScalings == 0 ? 1 : 0;
   it.it = 0;
+  it.action = kActNone;
   it.status = kActive;
 }
 
-// Zero state, p = G (optional learned[0] = G), q = mean(p), start.
-__device__ void reset_state(Item& it, const double* G) {
-  double acc[1] = {0.0};
-  for (int i = threadIdx.x; i < it.I; i += blockDim.x) {
+// Zero the item's slice of the state with p = G; returns the slice's sum of G.
+__device__ double reset_slice(Item& it, const double* G, int rank, int nblk) {
+  double sum = 0.0;
+  ITEM_LOOP(i, it.I) {
     const double pi = G[i];
     it.u[i] = 0.0;
     it.la[i] = 0.0;
@@ -553,77 +712,81 @@ __device__ void reset_state(Item& it, const double* G) {
     it.logp[i] = log(pi);
     it.wrow[i] = 0.f;
     it.orow[i] = 0.f;
-    acc[0] += pi;
+    sum += pi;
   }
-  for (int j = threadIdx.x; j < it.J; j += blockDim.x) {
+  ITEM_LOOP(j, it.J) {
     it.v[j] = 0.0;
     it.lb[j] = 0.0;
     it.lb_old[j] = 0.0;
     it.wcol[j] = 0.f;
     it.ocol[j] = 0.f;
   }
-  block_sum<1>(acc);
-  if (threadIdx.x == 0) {
-    it.q = acc[0] / (double)it.I;
-    start_solve(it);
-  }
-  __syncthreads();
+  return sum;
+}
+
+// Deterministic total of the item's per-CTA partials (fixed order).
+__device__ __forceinline__ double item_total(const BatchArgs& B, const Item& it, int q) {
+  double t = 0.0;
+  for (int b = 0; b < it.nblk; ++b) t += __ldcg(&B.part[(int64_t)(it.first_blk + b) * kNq + q]);
+  return t;
 }
 
 __global__ void __launch_bounds__(kThreads) init_kernel(BatchArgs B, const double* const* G) {
-  Item& it = B.items[blockIdx.x];
-  const double* g = G[blockIdx.x];
-  if (it.learned)
-    for (int i = threadIdx.x; i < it.I; i += blockDim.x) it.learned[i] = g[i];
-  // padding of the weight vectors stays 0 (read by the staged passes)
-  const int wr = (it.I + 3) & ~3, wc = (it.J + 3) & ~3;
-  for (int i = it.I + threadIdx.x; i < wr; i += blockDim.x) it.wrow[i] = 0.f;
-  for (int j = it.J + threadIdx.x; j < wc; j += blockDim.x) it.wcol[j] = 0.f;
-  if (threadIdx.x == 0) {
+  const ItemBlock ib = B.blk[blockIdx.x];
+  Item& it = B.items[ib.item];
+  const int rank = ib.rank, nblk = it.nblk;
+  const double* g = G[ib.item];
+  if (it.learned) ITEM_LOOP(i, it.I) it.learned[i] = g[i];
+  if (rank == 0) {
+    // padding of the weight vectors stays 0 (read by the staged passes)
+    const int wr = (it.I + 3) & ~3, wc = (it.J + 3) & ~3;
+    for (int i = it.I + threadIdx.x; i < wr; i += blockDim.x) it.wrow[i] = 0.f;
+    for (int j = it.J + threadIdx.x; j < wc; j += blockDim.x) it.wcol[j] = 0.f;
+  }
+  double acc[1] = {reset_slice(it, g, rank, nblk)};
+  block_sum<1>(acc);
+  if (threadIdx.x == 0) B.part[(int64_t)blockIdx.x * kNq] = acc[0];
+  if (arrive_last(B.item_ctr + ib.item, nblk) && threadIdx.x == 0) {
+    it.q = item_total(B, it, 0) / (double)it.I;
     it.gi = 0;
     it.it_total = 0;
     it.checks = 0;
     it.absorptions = 0;
     it.hit_max_iter = 0;
+    start_solve(it);
   }
-  __syncthreads();
-  reset_state(it, g);
-  if (last_block(B.counters + 5)) {
-    build_iter_lists(B);
-    if (threadIdx.x == 0) {
-      B.counters[0] = 0;
-      B.counters[1] = 0;
-      B.counters[2] = 0;
-      B.active[0] = B.n_items;
-    }
+  if (arrive_last(B.counters + 5, gridDim.x)) {
+    finish_body(B);
+    if (threadIdx.x == 0) B.counters[2] = 0;
   }
 }
 
 // After the two half-steps: tau-absorption (optimal_transport.py:137-141),
 // iteration / batch counting, max_iter (:143-145).
 __global__ void __launch_bounds__(kThreads) item_kernel(BatchArgs B) {
-  Item& it = B.items[blockIdx.x];
+  const ItemBlock ib = B.blk[blockIdx.x];
+  Item& it = B.items[ib.item];
+  const int rank = ib.rank, nblk = it.nblk;
   if (it.status == kActive) {
     const int par = it.parity;
     const double mx = __longlong_as_double((long long)it.maxslot[par]);
     const bool absorb = mx > it.tau;
     if (absorb) {
       const double eps = it.c.eps, inv_eps = it.c.inv_eps;
-      for (int i = threadIdx.x; i < it.I; i += blockDim.x) {
+      ITEM_LOOP(i, it.I) {
         const double un = it.u[i] + eps * it.la[i];
         it.u[i] = un;
         it.la[i] = 0.0;
         it.wrow[i] = (float)(un * inv_eps * kLog2e);
       }
-      for (int j = threadIdx.x; j < it.J; j += blockDim.x) {
+      ITEM_LOOP(j, it.J) {
         const double vn = it.v[j] + eps * it.lb[j];
         it.v[j] = vn;
         it.lb[j] = 0.0;
         it.wcol[j] = (float)(vn * inv_eps * kLog2e);
       }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    if (arrive_last(B.item_ctr + ib.item, nblk) && threadIdx.x == 0) {
       it.maxslot[par ^ 1] = 0ull;
       if (absorb) it.absorptions += 1;
       it.skip_row = 0;
@@ -639,212 +802,202 @@ __global__ void __launch_bounds__(kThreads) item_kernel(BatchArgs B) {
       }
     }
   }
-  if (last_block(B.counters + 3)) {
+  if (arrive_last(B.counters + 3, gridDim.x)) {
     build_check_lists(B);
     if (threadIdx.x == 0) B.counters[2] = 0;
   }
 }
 
-// End of a solve: the next growth iteration (G = row sums of this map) or the
-// outputs. log_scale = 0 for the reference's max_iter return R, -log J otherwise.
-__device__ void finish(Item& it, bool maxiter) {
-  const Coef c = it.c;
-  const double log_scale = maxiter ? 0.0 : -c.logJ;
-  if (it.gi + 1 < it.growth_iters) {
-    double* nextG = it.learned ? it.learned + (int64_t)(it.gi + 1) * it.I : it.rsum;
-    for (int i = threadIdx.x; i < it.I; i += blockDim.x)
-      nextG[i] = exp(it.la[i] + it.u[i] * c.inv_eps + it.Lrow[i] + log_scale);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      it.it_total += it.it;
-      it.gi += 1;
-    }
-    reset_state(it, nextG);
-    return;
-  }
-  for (int i = threadIdx.x; i < it.I; i += blockDim.x) {
-    it.row_sums[i] = exp(it.la[i] + it.u[i] * c.inv_eps + it.Lrow[i] + log_scale);
-    it.ubar[i] = it.u[i] + c.eps * it.la[i];
-  }
-  for (int j = threadIdx.x; j < it.J; j += blockDim.x) it.vbar[j] = it.v[j] + c.eps * it.lb[j];
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    it.it_total += it.it;
-    it.status = maxiter ? kDoneMaxIter : kDone;
-  }
-  __syncthreads();
-}
-
-// Next epsilon stage (optimal_transport.py:118-125): absorb with the old
-// epsilon, a = b = 1, new coefficients; offsets scaled by eps_old / eps_new.
-__device__ void next_stage(Item& it) {
-  const double eps_old = it.eps_i;
-  const double eps_new = eps_old / it.scale_factor;
-  const double inv_new = 1.0 / eps_new;
-  const float ratio = (float)(eps_old / eps_new);
-  for (int i = threadIdx.x; i < it.I; i += blockDim.x) {
-    const double un = it.u[i] + eps_old * it.la[i];
-    it.u[i] = un;
-    it.la[i] = 0.0;
-    it.la_old[i] = 0.0;
-    it.wrow[i] = (float)(un * inv_new * kLog2e);
-    it.orow[i] *= ratio;
-  }
-  for (int j = threadIdx.x; j < it.J; j += blockDim.x) {
-    const double vn = it.v[j] + eps_old * it.lb[j];
-    it.v[j] = vn;
-    it.lb[j] = 0.0;
-    it.lb_old[j] = 0.0;
-    it.wcol[j] = (float)(vn * inv_new * kLog2e);
-    it.ocol[j] *= ratio;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    it.eps_i = eps_new;
-    it.c = make_coef(eps_new, it.lambda1, it.lambda2, it.cost_scale, it.I, it.J, it.q);
-    it.maxslot[0] = 0ull;
-    it.maxslot[1] = 0ull;
-    it.parity = 0;
-    it.skip_row = 0;
-    it.stage += 1;
-    it.batch_cnt = 0;
-    it.due = 0;
-    it.gap = INFINITY;
-    const bool final = it.stage == kScalings;
-    it.threshold = final ? it.tolerance : 1e-6;
-    if (final) it.need_sumk = 1;
-  }
-  __syncthreads();
-}
-
 // Python's max(x, y): x unless y > x.
 __device__ __forceinline__ double py_max(double x, double y) { return (y > x) ? y : x; }
 
-// Stage-exit test / duality gap (optimal_transport.py:146-164) and the
-// transitions that follow from it.
+// Stage-exit test / duality gap (optimal_transport.py:146-164), sum exp(-C/eps)
+// of a new final stage, and the decision that follows (applied by apply_kernel).
+// Partials: [0..6] gap terms or [0..3] stage-test terms, [7] sum of the row
+// sums of the current coupling (next growth), [8] sum exp(-C/eps).
 __global__ void __launch_bounds__(kThreads) test_kernel(BatchArgs B) {
-  Item& it = B.items[blockIdx.x];
+  const ItemBlock ib = B.blk[blockIdx.x];
+  Item& it = B.items[ib.item];
+  const int rank = ib.rank, nblk = it.nblk;
   const int st = it.status;
-  if (st == kActive || st == kMaxIterPending) {
-    if (st == kActive && it.need_sumk == 1) {
-      double acc[1] = {0.0};
-      for (int i = threadIdx.x; i < it.I; i += blockDim.x) acc[0] += it.rsum[i];
-      block_sum<1>(acc);
-      if (threadIdx.x == 0) {
-        it.sumK = acc[0];
+  const bool sumk = st == kActive && it.need_sumk == 1;
+  const bool due = st == kActive && it.due;
+  if (sumk || due || st == kMaxIterPending) {
+    const Coef c = it.c;
+    const bool final = it.stage == kScalings;
+    double acc[kNq];
+#pragma unroll
+    for (int q = 0; q < kNq; ++q) acc[q] = 0.0;
+    if (sumk) ITEM_LOOP(i, it.I) acc[8] += it.rsum[i];
+    if (st == kMaxIterPending) {
+      ITEM_LOOP(i, it.I) acc[7] += exp(it.la[i] + it.u[i] * c.inv_eps + it.Lrow[i]);
+    } else if (due && final) {
+      ITEM_LOOP(i, it.I) {
+        const double ui = it.u[i], lai = it.la[i], pi = it.p[i];
+        const double x = exp(lai + ui * c.inv_eps + it.Lrow[i] - c.logJ);
+        const double ub = ui + c.eps * lai;
+        const double at = exp(lai) * exp(ui * c.inv_eps);
+        const double f = x * log(x / pi) - x + pi;
+        const double conj = c.lambda1 * pi * (exp(-c.eps * log(at) / c.lambda1) - 1.0);
+        acc[0] += c.lambda1 * f + conj + ub * x;
+        acc[2] += f;
+        acc[4] += ub * x;
+        acc[6] += x;
+      }
+      ITEM_LOOP(j, it.J) {
+        const double vj = it.v[j], lbj = it.lb[j];
+        const double y = exp(lbj + vj * c.inv_eps + it.Lcol[j] - c.logI);
+        const double vb = vj + c.eps * lbj;
+        const double bt = exp(lbj) * exp(vj * c.inv_eps);
+        const double f = y * log(y / c.q) - y + c.q;
+        const double conj = c.lambda2 * c.q * (exp(-c.eps * log(bt) / c.lambda2) - 1.0);
+        acc[1] += c.lambda2 * f + conj + vb * y;
+        acc[3] += f;
+        acc[5] += vb * y;
+      }
+      acc[7] = acc[6];
+    } else if (due) {
+      ITEM_LOOP(i, it.I) {
+        const double e = exp(it.u[i] * c.inv_eps);
+        const double ta = exp(it.la[i]) * e;
+        const double d = ta - exp(it.la_old[i]) * e;
+        acc[0] += d * d;
+        acc[1] += ta * ta;
+      }
+      ITEM_LOOP(j, it.J) {
+        const double e = exp(it.v[j] * c.inv_eps);
+        const double tb = exp(it.lb[j]) * e;
+        const double d = tb - exp(it.lb_old[j]) * e;
+        acc[2] += d * d;
+        acc[3] += tb * tb;
+      }
+    }
+    block_sum<kNq>(acc);
+    if (threadIdx.x < kNq) B.part[(int64_t)blockIdx.x * kNq + threadIdx.x] = acc[threadIdx.x];
+    if (arrive_last(B.item_ctr + ib.item, nblk) && threadIdx.x == 0) {
+      double t[kNq];
+      for (int q = 0; q < kNq; ++q) t[q] = item_total(B, it, q);
+      if (sumk) {
+        it.sumK = t[8];
         it.need_sumk = 0;
       }
-      __syncthreads();
-    }
-    if (st == kMaxIterPending) {
-      finish(it, true);
-    } else if (it.due) {
-      const Coef c = it.c;
-      const bool final = it.stage == kScalings;
-      double gap;
-      if (final) {
-        double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-        for (int i = threadIdx.x; i < it.I; i += blockDim.x) {
-          const double ui = it.u[i], lai = it.la[i], pi = it.p[i];
-          const double x = exp(lai + ui * c.inv_eps + it.Lrow[i] - c.logJ);
-          const double ub = ui + c.eps * lai;
-          const double at = exp(lai) * exp(ui * c.inv_eps);
-          const double f = x * log(x / pi) - x + pi;
-          const double conj = c.lambda1 * pi * (exp(-c.eps * log(at) / c.lambda1) - 1.0);
-          acc[0] += c.lambda1 * f + conj + ub * x;
-          acc[2] += f;
-          acc[4] += ub * x;
-          acc[6] += x;
+      if (st == kMaxIterPending) {
+        it.action = kActFinishMax;
+        it.q_next = t[7] / (double)it.I;
+      } else if (due) {
+        double gap;
+        if (final) {
+          const double I = (double)it.I, J = (double)it.J;
+          const double dx = 1.0 / I, dy = 1.0 / J;
+          const double gap_abs = dx * t[0] + dy * t[1];
+          const double pri = c.lambda1 * dx * t[2] + c.lambda2 * dy * t[3] + dx * t[4] + dy * t[5] +
+                             it.eps_i * (it.sumK / (I * J) - dx * t[6]);
+          gap = gap_abs / fabs(pri);
+        } else {
+          gap = py_max(sqrt(t[0]) / (1.0 + sqrt(t[1])), sqrt(t[2]) / (1.0 + sqrt(t[3])));
         }
-        for (int j = threadIdx.x; j < it.J; j += blockDim.x) {
-          const double vj = it.v[j], lbj = it.lb[j];
-          const double y = exp(lbj + vj * c.inv_eps + it.Lcol[j] - c.logI);
-          const double vb = vj + c.eps * lbj;
-          const double bt = exp(lbj) * exp(vj * c.inv_eps);
-          const double f = y * log(y / c.q) - y + c.q;
-          const double conj = c.lambda2 * c.q * (exp(-c.eps * log(bt) / c.lambda2) - 1.0);
-          acc[1] += c.lambda2 * f + conj + vb * y;
-          acc[3] += f;
-          acc[5] += vb * y;
-        }
-        block_sum<7>(acc);
-        const double I = (double)it.I, J = (double)it.J;
-        const double dx = 1.0 / I, dy = 1.0 / J;
-        const double gap_abs = dx * acc[0] + dy * acc[1];
-        const double pri = c.lambda1 * dx * acc[2] + c.lambda2 * dy * acc[3] + dx * acc[4] + dy * acc[5] +
-                           it.eps_i * (it.sumK / (I * J) - dx * acc[6]);
-        gap = gap_abs / fabs(pri);
-      } else {
-        double acc[4] = {0, 0, 0, 0};
-        for (int i = threadIdx.x; i < it.I; i += blockDim.x) {
-          const double e = exp(it.u[i] * c.inv_eps);
-          const double ta = exp(it.la[i]) * e;
-          const double d = ta - exp(it.la_old[i]) * e;
-          acc[0] += d * d;
-          acc[1] += ta * ta;
-        }
-        for (int j = threadIdx.x; j < it.J; j += blockDim.x) {
-          const double e = exp(it.v[j] * c.inv_eps);
-          const double tb = exp(it.lb[j]) * e;
-          const double d = tb - exp(it.lb_old[j]) * e;
-          acc[2] += d * d;
-          acc[3] += tb * tb;
-        }
-        block_sum<4>(acc);
-        gap = py_max(sqrt(acc[0]) / (1.0 + sqrt(acc[1])), sqrt(acc[2]) / (1.0 + sqrt(acc[3])));
-      }
-      const bool cont = gap > it.threshold;
-      __syncthreads();
-      if (threadIdx.x == 0) {
         it.checks += 1;
         it.due = 0;
         it.batch_cnt = 0;
         it.gap = gap;
-      }
-      __syncthreads();
-      if (cont) {
-        if (final) {
-          // The check's row sums are the next iteration's first half-step:
-          // apply its a-update now and skip that row pass.
-          double amax = 0.0;
-          for (int i = threadIdx.x; i < it.I; i += blockDim.x) amax = fmax(amax, item_a_update(it, i, it.Lrow[i]));
-          amax = block_max(amax);
-          if (threadIdx.x == 0) {
-            atomic_max_nonneg(&it.maxslot[it.parity], amax);
+        if (gap > it.threshold) {
+          if (final) {
+            // The check's row sums are the next iteration's first half-step:
+            // apply_kernel applies its a-update and the row pass is skipped.
+            it.action = kActCont;
             it.skip_row = 1;
           }
-        }
-      } else if (!final) {
-        next_stage(it);
-      } else if (isnan(gap)) {
-        if (threadIdx.x == 0) {
+        } else if (!final) {
+          // Next epsilon stage (optimal_transport.py:118-125); vectors in apply_kernel.
+          it.eps_prev = it.eps_i;
+          it.eps_i = it.eps_i / it.scale_factor;
+          it.c = make_coef(it.eps_i, it.lambda1, it.lambda2, it.cost_scale, it.I, it.J, it.q);
+          it.maxslot[0] = 0ull;
+          it.maxslot[1] = 0ull;
+          it.parity = 0;
+          it.skip_row = 0;
+          it.stage += 1;
+          it.gap = INFINITY;
+          it.threshold = it.stage == kScalings ? it.tolerance : 1e-6;
+          if (it.stage == kScalings) it.need_sumk = 1;
+          it.action = kActStage;
+        } else if (isnan(gap)) {
           it.it_total += it.it;
           it.status = kNonfinite;
+        } else {
+          it.action = kActFinish;
+          it.q_next = t[7] / (double)it.I;
         }
-      } else {
-        finish(it, false);
       }
     }
   }
-  if (last_block(B.counters + 4)) {
-    build_iter_lists(B);
-    __shared__ int cnt[kWarps];
-    int n = 0;
-    for (int k = threadIdx.x; k < B.n_items; k += blockDim.x) {
-      const int s = __ldcg(&B.items[k].status);
-      n += (s == kActive || s == kMaxIterPending) ? 1 : 0;
+}
+
+// The vector work of test_kernel's decisions, then the next iteration's lists.
+__global__ void __launch_bounds__(kThreads) apply_kernel(BatchArgs B) {
+  const ItemBlock ib = B.blk[blockIdx.x];
+  Item& it = B.items[ib.item];
+  const int rank = ib.rank, nblk = it.nblk;
+  const int act = it.action;
+  if (act != kActNone) {
+    const Coef c = it.c;
+    if (act == kActCont) {
+      double lmax = -INFINITY;
+      ITEM_LOOP(i, it.I) lmax = fmax(lmax, item_a_update(it, i, it.Lrow[i]));
+      lmax = block_max(lmax);
+      if (threadIdx.x == 0) atomic_max_nonneg(&it.maxslot[it.parity], exp(lmax));
+    } else if (act == kActStage) {
+      // absorb with the old epsilon, a = b = 1; offsets scale with 1/eps
+      const double eps_old = it.eps_prev;
+      const double inv_new = 1.0 / it.eps_i;
+      const float ratio = (float)(eps_old / it.eps_i);
+      ITEM_LOOP(i, it.I) {
+        const double un = it.u[i] + eps_old * it.la[i];
+        it.u[i] = un;
+        it.la[i] = 0.0;
+        it.la_old[i] = 0.0;
+        it.wrow[i] = (float)(un * inv_new * kLog2e);
+        it.orow[i] *= ratio;
+      }
+      ITEM_LOOP(j, it.J) {
+        const double vn = it.v[j] + eps_old * it.lb[j];
+        it.v[j] = vn;
+        it.lb[j] = 0.0;
+        it.lb_old[j] = 0.0;
+        it.wcol[j] = (float)(vn * inv_new * kLog2e);
+        it.ocol[j] *= ratio;
+      }
+    } else {
+      // End of a solve: the reference returns R / J, or R at max_iter.
+      const double log_scale = act == kActFinishMax ? 0.0 : -c.logJ;
+      if (it.gi + 1 < it.growth_iters) {
+        // next growth iteration: G = row sums of this coupling, fresh state
+        double* nextG = it.learned ? it.learned + (int64_t)(it.gi + 1) * it.I : it.rsum;
+        ITEM_LOOP(i, it.I) nextG[i] = exp(it.la[i] + it.u[i] * c.inv_eps + it.Lrow[i] + log_scale);
+        reset_slice(it, nextG, rank, nblk);
+      } else {
+        ITEM_LOOP(i, it.I) {
+          it.row_sums[i] = exp(it.la[i] + it.u[i] * c.inv_eps + it.Lrow[i] + log_scale);
+          it.ubar[i] = it.u[i] + c.eps * it.la[i];
+        }
+        ITEM_LOOP(j, it.J) it.vbar[j] = it.v[j] + c.eps * it.lb[j];
+      }
     }
-    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
-    if ((threadIdx.x & 31) == 0) cnt[threadIdx.x >> 5] = n;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int t = 0;
-      for (int w = 0; w < kWarps; ++w) t += cnt[w];
-      B.active[0] = t;
-      B.counters[0] = 0;
-      B.counters[1] = 0;
+    if (arrive_last(B.item_ctr + ib.item, nblk) && threadIdx.x == 0) {
+      if (act == kActFinish || act == kActFinishMax) {
+        it.it_total += it.it;
+        if (it.gi + 1 < it.growth_iters) {
+          it.gi += 1;
+          it.q = it.q_next;
+          start_solve(it);
+        } else {
+          it.status = act == kActFinishMax ? kDoneMaxIter : kDone;
+        }
+      }
+      it.action = kActNone;
     }
   }
+  if (arrive_last(B.counters + 7, gridDim.x)) finish_body(B);
 }
 
 // ---------------------------------------------------------------------------
@@ -913,7 +1066,16 @@ static std::vector<Tile> make_tiles(const std::vector<int>& rows, const std::vec
   return out;
 }
 
+// CTAs of the per-item kernels for an item of I + J points.
+static inline int item_blocks(int64_t I, int64_t J) {
+  return (int)std::min<int64_t>(32, std::max<int64_t>(1, (I + J + 2047) / 2048));
+}
+
 struct Layout {
+  ItemBlock* blk;
+  int nblk;
+  int* item_ctr;
+  double* part;
   Item* items;
   Seg* segs;
   Tile* tiles[2][2];  // [dir][rw - 1]
@@ -933,6 +1095,11 @@ static size_t layout(char* base, const wotg_pair* pairs, int np, const wotg_item
                      std::vector<Item>* host_items) {
   Bump b{base, 0};
   L.items = b.take<Item>(ni);
+  L.nblk = 0;
+  for (int k = 0; k < ni; ++k) L.nblk += item_blocks(pairs[items[k].pair].I, pairs[items[k].pair].J);
+  L.blk = b.take<ItemBlock>(L.nblk);
+  L.item_ctr = b.take<int>(ni);
+  L.part = b.take<double>((size_t)L.nblk * kNq);
   L.segs = b.take<Seg>(2 * (size_t)np);
   int64_t maxcols = 4;
   std::vector<int> rows0(np), cols0(np), kp(np, 0);
@@ -1156,6 +1323,7 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
     for (int k = 0; k < ni; ++k) pair_items[fill[items[k].pair]++] = k;
   }
   std::vector<const double*> G(ni);
+  std::vector<ItemBlock> blk;
   long long work = 0;
   for (int k = 0; k < ni; ++k) {
     const wotg_item& in = items[k];
@@ -1180,6 +1348,9 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
     it.row_sums = row_sums + in.row_offset;
     it.learned = learned_growth ? learned_growth + in.growth_offset : nullptr;
     it.c.kappa2 = (float)(pr.cost_scale / P.epsilon * kLog2e);
+    it.first_blk = (int)blk.size();
+    it.nblk = item_blocks(pr.I, pr.J);
+    for (int r = 0; r < it.nblk; ++r) blk.push_back(ItemBlock{k, r});
     G[k] = pr.G;
     work += (long long)pr.I * pr.J;
   }
@@ -1231,12 +1402,16 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
   WOTG_BCUDA(cudaMemcpyAsync(L.pair_off, pair_off.data(), sizeof(int) * (np + 1), cudaMemcpyHostToDevice, cs));
   WOTG_BCUDA(cudaMemcpyAsync(L.G, G.data(), sizeof(double*) * ni, cudaMemcpyHostToDevice, cs));
   WOTG_BCUDA(cudaMemsetAsync(L.counters, 0, 8 * sizeof(int), cs));
+  WOTG_BCUDA(cudaMemsetAsync(L.item_ctr, 0, ni * sizeof(int), cs));
+  WOTG_BCUDA(cudaMemcpyAsync(L.blk, blk.data(), sizeof(ItemBlock) * blk.size(), cudaMemcpyHostToDevice, cs));
   size_t maxcols = 4;
   for (int p = 0; p < np; ++p) maxcols = std::max<size_t>(maxcols, round4(std::max(pairs[p].I, pairs[p].J)));
   WOTG_BCUDA(cudaMemsetAsync(L.zeros, 0, maxcols * sizeof(float), cs));
 
-  BatchArgs B{L.items,   ni,        np,        L.pair_items, L.pair_off, L.row_n, L.row_list, L.col_n,
-              L.col_list, L.chk_n, L.chk_list, L.counters,  L.active,   L.zeros};
+  BatchArgs B{L.items,  ni,         np,      L.pair_items, L.pair_off, L.row_n, L.row_list,
+              L.col_n,  L.col_list, L.chk_n, L.chk_list,   L.counters, L.active, L.zeros,
+              L.blk,    L.item_ctr, L.part};
+  const int nblk = L.nblk;
 
   // The check list has 2 K_p slots per pair: its offsets are 2 * pair_off.
   int* chk_off = probe_off;
@@ -1273,7 +1448,7 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
     }
   }
 
-  init_kernel<<<ni, kThreads, 0, cs>>>(B, L.G);
+  init_kernel<<<nblk, kThreads, 0, cs>>>(B, L.G);
   WOTG_LAUNCHED();
 
   const PassCfg& c0 = kCfgs[cfg[0]];
@@ -1290,9 +1465,10 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
   for (int b = 0; b < kBodies; ++b) {
     c0.spec<<<grid_row, kThreads, 0, cs>>>(Arow);
     c1.spec<<<grid_col, kThreads, 0, cs>>>(Acol);
-    item_kernel<<<ni, kThreads, 0, cs>>>(B);
+    item_kernel<<<nblk, kThreads, 0, cs>>>(B);
     c0.spec<<<grid_row, kThreads, 0, cs>>>(Achk);
-    test_kernel<<<ni, kThreads, 0, cs>>>(B);
+    test_kernel<<<nblk, kThreads, 0, cs>>>(B);
+    apply_kernel<<<nblk, kThreads, 0, cs>>>(B);
   }
   {
     cudaError_t e = cudaStreamEndCapture(cs, &graph);
@@ -1315,7 +1491,7 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
   for (;;) {
     const int slot = (int)(launched & 1);
     WOTG_BCUDA(cudaGraphLaunch(exec, cs));
-    for (int q = 0; q < kBodies * 5; ++q) count_launch();
+    for (int q = 0; q < kBodies * 6; ++q) count_launch();
     WOTG_BCUDA(cudaMemcpyAsync(pinned + slot, L.active, sizeof(int), cudaMemcpyDeviceToHost, cs));
     WOTG_BCUDA(cudaEventRecord(ev_done[slot], cs));
     ++launched;
