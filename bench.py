@@ -46,6 +46,10 @@ def parse():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--pair', default=None, help='I,J cells of a smaller pair (profiling runs)')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--workload', default='pair', choices=['pair', 'course'],
+                    help="pair: one 20000x25000 map per step; course: the batched 41-day time course x "
+                         "5x5 epsilon/lambda1 sweep (1000 maps) per step")
+    ap.add_argument('--course-days', type=int, default=41)
     ap.add_argument('--form', default='auto', choices=['materialized', 'onthefly', 'auto'],
                     help='materialised FP32 cost stream or tensor-core cost recomputation')
     return ap.parse_args()
@@ -190,9 +194,154 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+
+COURSE_EPS = (0.01, 0.025, 0.05, 0.075, 0.1)
+COURSE_L1 = (0.1, 0.3, 1, 3, 10)
+COURSE_CFG = dict(growth_iters=1, lambda2=50, epsilon0=1, tau=10000, scaling_iter=3000, inner_iter_max=50,
+                  tolerance=1e-8, max_iter=1e7, batch_size=5, extra_iter=1000)
+
+
+def course_days(n_days, seed=0):
+    """Per-day cells of the long synthetic time course (day sizes log-uniform in
+    [1000, 30000]), generated in a spawn process pool before any CUDA call."""
+    import multiprocessing as mp
+    from wot_gb300 import synthetic
+    sizes = synthetic.log_uniform_day_sizes(n_days, 1000, 30000, seed=2)
+    prof = synthetic.course_profiles(n_days, GENES, CLUSTERS, seed)
+    with mp.get_context('spawn').Pool(min(16, os.cpu_count() or 1)) as pool:
+        days = pool.starmap(synthetic.course_day, [(prof, t, int(n)) for t, n in enumerate(sizes)])
+    return sizes, days
+
+
+def run_course(args, days_data):
+    """The batched workload: every consecutive day pair x the 5 x 5 epsilon x
+    lambda1 grid in one wotg_solve_batched call per step; the plain driver on
+    the items of a stratified subset of pairs (and the batched solver on the same
+    subset) for the batched-vs-plain ratio."""
+    import torch
+    from wot_gb300 import _build, _native
+    from wot_gb300.ot import batch as Bt, device as D
+    from wot_gb300.ot.util import compute_pca
+    import logging
+    logging.disable(logging.WARNING)
+    _build.build()
+    lib = _native.load()
+    sizes, days = days_data
+    npairs = len(days) - 1
+    pairs, pts = [], []
+    for t in range(npairs):
+        x0, x1, sv, _ = compute_pca(days[t][0], days[t + 1][0], PCA_D)
+        a, b = (x0 * sv).float().contiguous(), (x1 * sv).float().contiguous()
+        cost = D.default_cost(a, b)
+        pairs.append(Bt.prepare_pair(cost, days[t][1]))   # G = growth ** (t1 - t0), t1 - t0 = 1
+        pts.append((a, b))
+    items = [(p, dict(COURSE_CFG, epsilon=e, lambda1=l)) for p in range(npairs) for e in COURSE_EPS for l in COURSE_L1]
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        maps = Bt.solve_batched(pairs, items)
+    torch.cuda.synchronize()
+    n_launch0 = lib.wotg_launch_count()
+    with Clocks(0) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            maps = Bt.solve_batched(pairs, items)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.wotg_launch_count() - n_launch0
+    t = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    its = np.array([m.stats['iterations'] for m in maps], dtype=np.float64)
+    ij = np.array([m.shape[0] * m.shape[1] for m in maps], dtype=np.float64)
+    work = float(np.sum(its * ij * 2))
+
+    # plain driver, item by item, on a stratified subset of pairs (by I*J)
+    order = np.argsort([p.cost.I * p.cost.J for p in pairs])
+    subset = sorted({int(order[int(q * (npairs - 1))]) for q in (0.1, 0.35, 0.6, 0.85)})
+    sub_items = [(subset.index(p), c) for p, c in items if p in subset]
+    sub_pairs = [pairs[p] for p in subset]
+    Bt.solve_batched(sub_pairs, sub_items)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sub_maps = Bt.solve_batched(sub_pairs, sub_items)
+    torch.cuda.synchronize()
+    t_sub_batched = time.perf_counter() - t0
+    t_plain = {}
+    for form in ('auto', 'materialized'):
+        D.solve(sub_pairs[0].cost, sub_pairs[0].G, sub_items[0][1], 0, want_tmap=False, want_potentials=True,
+                form=form)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for p, c in sub_items:
+            D.solve(sub_pairs[p].cost, sub_pairs[p].G, c, 0, want_tmap=False, want_potentials=True, form=form)
+        torch.cuda.synchronize()
+        t_plain[form] = time.perf_counter() - t0
+    w_sub = float(sum(m.stats['iterations'] * m.shape[0] * m.shape[1] for m in sub_maps))
+    w_all = float(np.sum(its * ij))
+    best_plain = min(t_plain.values())
+
+    hbm_peak, tf_peak, peak_kind = peaks()
+    line = {'metric': METRIC, 'value': len(items) / t, 'unit': 'maps/s', 'n_gpus': 1, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': t * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': 'batched time course: %d days (log-uniform 1000-30000 cells, 1000 genes, '
+                                   '20 clusters, local_pca=30), %d consecutive pairs x eps %s x lambda1 %s, '
+                                   'lambda2=50, duality-gap solver; maps returned as potentials'
+                                   % (len(days), npairs, list(COURSE_EPS), list(COURSE_L1)),
+                       'pairs': npairs, 'items': len(items), 'cells': [int(n) for n in sizes],
+                       'l2': 'inputs larger than L2 (FP32 costs and transposes %.1f GB)'
+                             % (sum(p.cost.I * p.cost.ldc + p.cost.J * p.CT.stride(0) for p in pairs) * 4 / 1e9),
+                       'timed': 'one wotg_solve_batched call over all items, costs resident'},
+            'sinkhorn_iter_per_s': float(np.sum(its)) / t, 'iterations_per_map': float(np.mean(its)),
+            'max_iterations': int(its.max()),
+            'element_evaluations_per_s': work / t,
+            'batched_vs_plain': {
+                'subset_pairs': subset, 'subset_items': len(sub_items),
+                'batched_s': t_sub_batched, 'plain_auto_s': t_plain['auto'],
+                'plain_materialized_s': t_plain['materialized'],
+                'ratio_vs_best_plain': best_plain / t_sub_batched,
+                'plain_maps_per_s_extrapolated': len(items) / (best_plain * w_all / w_sub),
+                'ratio_full_extrapolated': (best_plain * w_all / w_sub) / t,
+                'note': 'plain = wotg_compute_transport_matrix per item (potentials out), the faster of the '
+                        'on-the-fly and materialised forms; full-course plain time extrapolated from the subset '
+                        'by sum(iterations * I * J)'},
+            'gpu_launches': int(launches), 'clocks': clk.summary(), 'peaks': {'kind': peak_kind}}
+    if not args.no_cpu:
+        # parity and CPU baseline: the oracle on three items of the smallest pair
+        from oracle import ot_model as oom, optimal_transport as oot
+        p = int(order[0])
+        a, b = (x.double().cpu().numpy() for x in pts[p])
+        C = oom.compute_default_cost_matrix(a, b)
+        G = days[p][1]
+        errs, t_cpu, w_cpu = [], 0.0, 0.0
+        for e, l in ((0.01, 0.1), (0.05, 1), (0.1, 10)):
+            k = items.index((p, dict(COURSE_CFG, epsilon=e, lambda1=l)))
+            st = {}
+            t0 = time.perf_counter()
+            R = oot.optimal_transport_duality_gap(C=C, G=G.copy(), stats=st, **dict(COURSE_CFG, epsilon=e, lambda1=l))
+            t_cpu += time.perf_counter() - t0
+            w_cpu += st['iterations'] * C.shape[0] * C.shape[1]
+            T = maps[k].dense().cpu().numpy()
+            errs.append({'eps': e, 'lambda1': l, 'coupling_max_rel_err': float(np.abs(T - R).max() / np.abs(R).max()),
+                         'row_marginal_max_rel_err': float(np.abs(T.sum(1) - R.sum(1)).max() / np.abs(R.sum(1)).max()),
+                         'col_marginal_max_rel_err': float(np.abs(T.sum(0) - R.sum(0)).max() / np.abs(R.sum(0)).max()),
+                         'iterations_gpu': int(maps[k].stats['iterations']), 'iterations_oracle': int(st['iterations'])})
+        line['parity_sample'] = {'pair': p, 'shape': list(C.shape), 'items': errs}
+        cpu_value = len(items) / (t_cpu * w_all / w_cpu)
+        line['cpu_baseline'] = {'value': cpu_value, 'unit': 'maps/s', 'cores': blas_threads(), 'kind': 'port',
+                                'sample': 'oracle FP64 solves of 3 items of the smallest pair (%dx%d, %.1f s); '
+                                          'extrapolated to all items by sum(iterations * I * J)' % (C.shape[0], C.shape[1], t_cpu)}
+    line['e2e'] = None
+    print(json.dumps(line), flush=True)
+
 def main():
     global I_FULL, J_FULL, WORKLOAD
     args = parse()
+    if args.workload == 'course' and args.impl != 'reference':
+        data = course_days(args.course_days)
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        run_course(args, data)
+        return
     if args.pair:
         I_FULL, J_FULL = (int(v) for v in args.pair.split(','))
         WORKLOAD = WORKLOAD.replace('20000x25000', '%dx%d' % (I_FULL, J_FULL))

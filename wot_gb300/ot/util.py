@@ -23,7 +23,8 @@ def compute_pca(m1, m2, n_components):
     """Returns ``(pca_1, pca_2, singular_values, mean_shift)`` as device tensors
     (FP64): pca_k are the components_.T rows of each day."""
     torch = N.require_cuda()
-    x = torch.cat([torch.as_tensor(dense(m1), device='cuda'), torch.as_tensor(dense(m2), device='cuda')])
+    x = torch.cat([torch.as_tensor(dense(m1), device='cuda', dtype=torch.float64),
+                   torch.as_tensor(dense(m2), device='cuda', dtype=torch.float64)])
     mean_shift = x.mean(dim=0)
     x = x - mean_shift
     n_components = min(int(n_components), x.shape[0])

@@ -96,3 +96,31 @@ def log_uniform_day_sizes(n_days, lo=1000, hi=30000, seed=2):
     """Per-day cell counts log-uniform in [lo, hi] (the batched time-course workload)."""
     rng = np.random.default_rng(seed)
     return np.exp(rng.uniform(np.log(lo), np.log(hi), size=n_days)).astype(np.int64)
+
+
+def course_profiles(n_days, n_genes=1000, n_clusters=20, seed=0, drift=0.1):
+    """Cluster profiles of a long time course: lognormal(sigma=1) cluster means,
+    per-day drift and per-day cluster weights, from one seeded stream."""
+    rng = np.random.default_rng(seed)
+    log_mu = rng.normal(0.0, 1.0, size=(n_clusters, n_genes))
+    log_drift = rng.normal(0.0, drift, size=(n_clusters, n_genes))
+    weights = rng.dirichlet(np.ones(n_clusters) * 2.0, size=n_days)
+    mu0 = np.exp(log_mu[rng.integers(0, n_clusters, size=2000)])
+    scale = _scale_for_zero_fraction(mu0, 0.9)
+    return {'log_mu': log_mu, 'log_drift': log_drift, 'weights': weights, 'scale': scale, 'seed': seed}
+
+
+def course_day(profiles, t, n, jitter=0.25):
+    """Cells of day t of a long time course (same generator as time_course, one
+    seeded stream per day so that days can be produced independently):
+    returns X (n x genes, log1p(CP10k)) and growth rates (lognormal(0, 0.3))."""
+    rng = np.random.default_rng([profiles['seed'], int(t) + 1])
+    log_mu, log_drift = profiles['log_mu'], profiles['log_drift']
+    k = rng.choice(log_mu.shape[0], size=int(n), p=profiles['weights'][t])
+    mu = np.exp(log_mu[k] + t * log_drift[k] + rng.normal(0.0, jitter, size=(int(n), log_mu.shape[1])))
+    mu *= profiles['scale']
+    counts = rng.negative_binomial(NB_SIZE, NB_SIZE / (NB_SIZE + mu)).astype(np.float32)
+    totals = np.maximum(counts.sum(axis=1, keepdims=True), 1.0)
+    X = np.log1p(counts / totals * 1e4).astype(np.float32)
+    growth = rng.lognormal(0.0, 0.3, size=int(n))
+    return X, growth
