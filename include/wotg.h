@@ -147,6 +147,15 @@ int wotg_compute_transport_matrix(const wotg_problem* problem, const wotg_params
                                   double* u_bar, double* v_bar, wotg_stats* stats,
                                   void* workspace, size_t workspace_bytes, void* stream);
 
+/* Warm-started fixed-epsilon iterations (no counterpart in the reference; its
+ * iterations at the final epsilon are optimal_transport.py:131-141): from the
+ * absorbed potentials (u_bar, v_bar, device, in/out), n_iter iterations of the
+ * reference's a/b updates with tau-absorption at `epsilon`, same problem and
+ * workspace as wotg_compute_transport_matrix. Polishes the potentials of a solve
+ * stopped on the duality gap towards the exact optimum (before wotg_ot_adjoint). */
+int wotg_refine_potentials(const wotg_problem* problem, const wotg_params* params, double epsilon, int32_t n_iter,
+                           double* u_bar, double* v_bar, void* workspace, size_t workspace_bytes, void* stream);
+
 /* wotg_compute_transport_matrix for callers that cannot call cudaMalloc (a host
  * whose device memory is owned by another allocator or pool, or a path where
  * cudaMalloc's implicit device synchronisation is not acceptable). No counterpart
@@ -277,6 +286,26 @@ int wotg_lse_matvec_multi(const float* C, int64_t I, int64_t J, int64_t ldc, con
 int wotg_coupling_from_potentials(const float* C, int64_t I, int64_t J, int64_t ldc, double cost_scale, double eps,
                                   const double* u_bar, const double* v_bar, double log_scale, double* out,
                                   void* stream);
+
+/* Gradient of the converged unbalanced entropic OT objective (no counterpart in
+ * the reference, which has no derivatives): the objective is the reference's
+ * dual at the optimum (optimal_transport.py:56-62, which its duality-gap test
+ * drives to the primal, :146-152),
+ *   D = -lambda1 dx sum_i p_i (e^(-u_bar_i/lambda1) - 1) - lambda2 dy q sum_j (e^(-v_bar_j/lambda2) - 1)
+ *       - eps/(I J) sum_ij (R_ij - K0_ij),
+ *   R_ij = exp((u_bar_i + v_bar_j - C_ij)/eps), K0_ij = exp(-C_ij/eps), C_ij = cost_scale |x_i - y_j|^2,
+ *   dx = 1/I, dy = 1/J, q = mean(p),
+ * differentiated by the envelope theorem at the converged potentials (u_bar,
+ * v_bar from a solve with the same cost, e.g. wotg_compute_transport_matrix):
+ * grad_x (I x d), grad_y (J x d, may be NULL), grad_p (I, may be NULL; the
+ * derivative through q = mean(p) included) FP64 on the device; *objective
+ * (HOST, may be NULL) = D. X, Y: FP32 points (row strides ldx, ldy), d <= 64;
+ * the cost is recomputed from them tile by tile, never stored. */
+size_t wotg_ot_adjoint_workspace_bytes(int64_t I, int64_t J);
+int wotg_ot_adjoint(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy, int32_t d,
+                    double cost_scale, double epsilon, double lambda1, double lambda2, const double* u_bar,
+                    const double* v_bar, const double* p, double* grad_x, double* grad_y, double* grad_p,
+                    double* objective, void* workspace, size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

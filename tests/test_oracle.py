@@ -107,3 +107,32 @@ def test_tmap_restatement_on_integer_maps(chain_golden):
     f = otm.fates(tmaps, tp, P, 4.0)
     assert f.shape == (4 + 2 + 5 + 6 + 3, 2)             # no 'Other': P covers every cell
     np.testing.assert_allclose(f.sum(axis=1), 1.0)
+
+
+def test_adjoint_reference_fixed_point_and_gradient():
+    """oracle/adjoint.py: its fixed-epsilon potential iteration converges to the
+    coupling of the reference's solver (numpy oracle at tolerance 1e-12), and
+    autograd through unrolled iterations from the optimum equals central finite
+    differences of the converged objective."""
+    torch = pytest.importorskip('torch')
+    from oracle import adjoint as A, optimal_transport as oot
+    rng = np.random.default_rng(0)
+    I, J, d = 40, 50, 3
+    x = torch.tensor(rng.normal(size=(I, d)))
+    y = torch.tensor(rng.normal(size=(J, d)))
+    logg = torch.tensor(rng.normal(0.0, 0.3, I))
+    scale = 1.0 / float(np.median(A.cost(x, y, 1.0).numpy()))
+    eps, l1, l2 = 0.1, 1.0, 50.0
+    D, ub, vb = A.objective(x, y, logg, eps, l1, l2, scale)
+    C = A.cost(x, y, scale).numpy()
+    R = oot.optimal_transport_duality_gap(C=C, G=np.exp(logg.numpy()), lambda1=l1, lambda2=l2, epsilon=eps,
+                                          batch_size=5, tolerance=1e-12, tau=1e4, epsilon0=1, max_iter=1e7)
+    T = np.exp((ub.numpy()[:, None] + vb.numpy()[None, :] - C) / eps) / J
+    assert np.abs(T - R).max() <= 1e-6 * np.abs(R).max()
+    D2, gx, gy, gl = A.unrolled_gradient(x, y, logg, eps, l1, l2, scale, ub, vb, n_unroll=30)
+    assert abs(D2 - D) <= 1e-10 * abs(D)
+    coords = [('x', (3, 1)), ('x', (17, 0)), ('y', (7, 2)), ('y', (41, 1)), ('logg', (5,)), ('logg', (30,))]
+    fd = A.fd_gradient(x, y, logg, eps, l1, l2, scale, coords, ub, vb, h=1e-5)
+    ad = [float({'x': gx, 'y': gy, 'logg': gl}[n][i]) for n, i in coords]
+    gmax = max(float(gx.abs().max()), float(gy.abs().max()), float(gl.abs().max()))
+    assert max(abs(a - f) for a, f in zip(ad, fd)) <= 1e-6 * gmax

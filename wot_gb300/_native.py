@@ -36,7 +36,8 @@ EXPORTS = (
     'wotg_compute_transport_matrix_noalloc', 'wotg_problem_workspace_bytes', 'wotg_tc_selftest',
     'wotg_lse_points_workspace_bytes', 'wotg_lse_points', 'wotg_transpose_cost', 'wotg_batch_workspace_bytes',
     'wotg_solve_batched', 'wotg_lse_matvec_multi_workspace_bytes', 'wotg_lse_matvec_multi',
-    'wotg_coupling_from_potentials',
+    'wotg_coupling_from_potentials', 'wotg_ot_adjoint_workspace_bytes', 'wotg_ot_adjoint',
+    'wotg_refine_potentials',
 )
 
 
@@ -121,6 +122,11 @@ def load(path: str | None = None) -> ctypes.CDLL:
         'wotg_lse_matvec_multi': (ctypes.c_int, [vp, i64, i64, i64, vp, i64, ctypes.POINTER(ctypes.c_float), i32,
                                                  vp, i64, vp, ctypes.c_size_t, vp]),
         'wotg_coupling_from_potentials': (ctypes.c_int, [vp, i64, i64, i64, dbl, dbl, vp, vp, dbl, vp, vp]),
+        'wotg_ot_adjoint_workspace_bytes': (ctypes.c_size_t, [i64, i64]),
+        'wotg_refine_potentials': (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params), dbl, i32, vp, vp,
+                                                  vp, ctypes.c_size_t, vp]),
+        'wotg_ot_adjoint': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, dbl, dbl, dbl, vp, vp, vp, vp, vp,
+                                           vp, ctypes.POINTER(dbl), vp, ctypes.c_size_t, vp]),
         'wotg_lse_matvec_workspace_bytes': (ctypes.c_size_t, [i64, i64, i64]),
         'wotg_lse_matvec': (ctypes.c_int, [vp, i64, i64, i64, vp, ctypes.c_float, i32, vp, vp, ctypes.c_size_t,
                                            vp]),

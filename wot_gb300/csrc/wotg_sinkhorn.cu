@@ -340,6 +340,24 @@ __global__ void init_kernel(Geom g, Vecs V, const double* __restrict__ G) {
   }
 }
 
+// Warm start from absorbed potentials: u = u_bar, v = v_bar, a = b = 1.
+__global__ void load_potentials_kernel(Geom g, Vecs V, const double* __restrict__ ubar,
+                                       const double* __restrict__ vbar, double inv_eps) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < g.I) {
+    V.u[idx] = ubar[idx];
+    V.la[idx] = 0.0;
+    V.la_old[idx] = 0.0;
+    V.wrow[idx] = (float)(ubar[idx] * inv_eps * kLog2e);
+  } else if (idx < g.I + g.J) {
+    const int64_t j = idx - g.I;
+    V.v[j] = vbar[j];
+    V.lb[j] = 0.0;
+    V.lb_old[j] = 0.0;
+    V.wcol[j] = (float)(vbar[j] * inv_eps * kLog2e);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Deterministic two-level FP64 reductions: kRedBlocks blocks write partials,
 // one block sums them.
@@ -1078,6 +1096,70 @@ extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wot
   }
   if (stats) *stats = total;
   return status;
+}
+
+// Warm-started fixed-epsilon iterations (no counterpart in the reference; its
+// iterations at the final epsilon are optimal_transport.py:131-141): from
+// absorbed potentials (u_bar, v_bar), n_iter iterations of the reference's a/b
+// updates with tau-absorption at `epsilon`, potentials written back in place.
+// Polishes a solve stopped on the duality gap towards the exact optimum (used
+// before differentiating the objective).
+extern "C" int wotg_refine_potentials(const wotg_problem* prob, const wotg_params* params, double epsilon,
+                                      int32_t n_iter, double* u_bar, double* v_bar, void* workspace,
+                                      size_t workspace_bytes, void* stream) {
+  if (!prob || !params || !u_bar || !v_bar || n_iter < 0 || !(epsilon > 0)) return WOTG_BADARG;
+  const wotg_params P = *params;
+  const int64_t I = prob->I, J = prob->J, ldc = prob->ldc;
+  if (I <= 0 || J <= 0 || ldc < J || (ldc & 3) || !prob->C || !prob->G) return WOTG_BADARG;
+  if ((reinterpret_cast<uintptr_t>(prob->C) & 15) != 0) return WOTG_BADARG;
+  if (tc_valid(prob) != WOTG_OK) return WOTG_BADARG;
+  if (!workspace || workspace_bytes < wotg_problem_workspace_bytes(prob)) return WOTG_WORKSPACE;
+  Geom g = make_geom(I, J, ldc);
+  Bump b{reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255)), 0};
+  b.take<double>(I);
+  Vecs V{};
+  layout(b, g, V);
+  cudaStream_t st = (cudaStream_t)stream;
+  Solver S{prob->C, g, V, st, prob->cost_scale, 0, TcState{}};
+  if (tc_requested(prob)) {
+    tc_layout(b, prob, S.tc);
+    WOTG_CUDA(cudaMemsetAsync(S.tc.err, 0, sizeof(int), st));
+    const float sigma = (float)std::sqrt(prob->cost_scale);
+    int s = tc_pack_points(prob->X, I, prob->ldx, prob->d, S.tc.kp, sigma, 0, S.tc.Xb, S.tc.normX, st);
+    if (s) return s;
+    s = tc_pack_points(prob->Y, J, prob->ldy, prob->d, S.tc.kp, sigma, 0, S.tc.Yb, S.tc.normY, st);
+    if (s) return s;
+  }
+  init_kernel<<<S.vec_blocks(std::max(I, ldc)), 256, 0, st>>>(g, V, prob->G);
+  WOTG_LAUNCHED();
+  double q = 0.0;
+  int s = S.mean_of(V.p, I, &q);
+  if (s) return s;
+  const Coef c = S.coef(epsilon, P, q);
+  load_potentials_kernel<<<S.vec_blocks(I + J), 256, 0, st>>>(g, V, u_bar, v_bar, c.inv_eps);
+  WOTG_LAUNCHED();
+  s = S.tc_prepare(c);
+  if (s) return s;
+  int parity = 0;
+  for (int it = 0; it < n_iter; ++it) {
+    s = S.iteration(c, false, parity);
+    if (s) return s;
+    s = S.absorb(c, P.tau, parity);
+    if (s) return s;
+    parity ^= 1;
+  }
+  s = S.outputs(c, false, nullptr, nullptr, u_bar, v_bar);
+  if (s) return s;
+  WOTG_CUDA(cudaStreamSynchronize(st));
+  if (S.tc.on) {
+    int err = 0;
+    WOTG_CUDA(cudaMemcpy(&err, S.tc.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+      set_last_message("tensor-core half-step: a bounded wait timed out");
+      return WOTG_CUDA_ERROR;
+    }
+  }
+  return WOTG_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -189,6 +189,53 @@ def solve(cost: DeviceCost, G, cfg: dict, solver: int = N.SOLVER_DUALITY_GAP, wa
                        u_bar=u_bar, v_bar=v_bar, stats=stats.as_dict(), status=status)
 
 
+def _problem(cost: DeviceCost, Gd, form: str):
+    prob = N.Problem(I=cost.I, J=cost.J, C=cost.C.data_ptr(), ldc=cost.ldc, cost_scale=float(cost.scale),
+                     G=Gd.data_ptr())
+    if resolve_form(cost, form) == N.FORM_ONTHEFLY:
+        prob.X, prob.ldx = cost.X.data_ptr(), cost.X.stride(0)
+        prob.Y, prob.ldy = cost.Y.data_ptr(), cost.Y.stride(0)
+        prob.d, prob.form = cost.X.shape[1], N.FORM_ONTHEFLY
+    return prob
+
+
+def refine(cost: DeviceCost, G, cfg: dict, u_bar, v_bar, eps: float, n_iter: int, form: str = 'materialized'):
+    """n_iter warm-started iterations at epsilon `eps` from absorbed potentials
+    (in place); polishes a duality-gap solve towards the exact optimum."""
+    torch = _torch()
+    lib = N.load()
+    params = make_params(cfg, N.SOLVER_DUALITY_GAP)
+    Gd = _dev_f64(G, torch).reshape(-1)
+    prob = _problem(cost, Gd, form)
+    nbytes = lib.wotg_problem_workspace_bytes(ctypes.byref(prob))
+    ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
+    N.check(lib.wotg_refine_potentials(ctypes.byref(prob), ctypes.byref(params), float(eps), int(n_iter),
+                                       u_bar.data_ptr(), v_bar.data_ptr(), ws.data_ptr(), nbytes, _stream()),
+            'wotg_refine_potentials')
+    return u_bar, v_bar
+
+
+def ot_adjoint(X, Y, cost_scale: float, eps: float, lambda1: float, lambda2: float, u_bar, v_bar, p,
+               want_y: bool = True, want_p: bool = True):
+    """(objective, grad_x, grad_y, grad_p) of the converged unbalanced OT dual at
+    the potentials (u_bar, v_bar); X, Y FP32 device points."""
+    torch = _torch()
+    lib = N.load()
+    I, d = X.shape
+    J = Y.shape[0]
+    gx = torch.empty((I, d), dtype=torch.float64, device='cuda')
+    gy = torch.empty((J, d), dtype=torch.float64, device='cuda') if want_y else None
+    gp = torch.empty(I, dtype=torch.float64, device='cuda') if want_p else None
+    nbytes = lib.wotg_ot_adjoint_workspace_bytes(I, J)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
+    obj = ctypes.c_double(0.0)
+    N.check(lib.wotg_ot_adjoint(X.data_ptr(), I, X.stride(0), Y.data_ptr(), J, Y.stride(0), d, float(cost_scale),
+                                float(eps), float(lambda1), float(lambda2), u_bar.data_ptr(), v_bar.data_ptr(),
+                                p.data_ptr(), gx.data_ptr(), N.ptr(gy), N.ptr(gp), ctypes.byref(obj),
+                                ws.data_ptr(), nbytes, _stream()), 'wotg_ot_adjoint')
+    return obj.value, gx, gy, gp
+
+
 def apply_coupling(X, P, transpose: bool, normalize: bool):
     """push (transpose=False): P @ X; pull (transpose=True): (X @ P.T).T; FP64 on device."""
     torch = _torch()
