@@ -46,7 +46,7 @@ def parse():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--pair', default=None, help='I,J cells of a smaller pair (profiling runs)')
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--workload', default='pair', choices=['pair', 'course'],
+    ap.add_argument('--workload', default='pair', choices=['pair', 'course', 'chain'],
                     help="pair: one 20000x25000 map per step; course: the batched 41-day time course x "
                          "5x5 epsilon/lambda1 sweep (1000 maps) per step")
     ap.add_argument('--course-days', type=int, default=41)
@@ -333,9 +333,156 @@ def run_course(args, days_data):
     line['e2e'] = None
     print(json.dumps(line), flush=True)
 
+
+CHAIN_CFG = dict(growth_iters=1, epsilon=0.05, lambda1=1, lambda2=50, epsilon0=1, tau=10000, scaling_iter=3000,
+                 inner_iter_max=50, tolerance=1e-8, max_iter=1e7, batch_size=5, extra_iter=1000)
+
+
+def chain_days(big=60000, n_chain=21, lo=20000, hi=60000, seed=4):
+    """Cells of the large pair (two days of `big` cells) and of a chain of
+    n_chain days with log-uniform sizes in [lo, hi], 1000 genes, 20 clusters."""
+    import multiprocessing as mp
+    from wot_gb300 import synthetic
+    sizes = [big, big] + [int(n) for n in synthetic.log_uniform_day_sizes(n_chain, lo, hi, seed=seed)]
+    prof = synthetic.course_profiles(len(sizes), GENES, CLUSTERS, seed)
+    with mp.get_context('spawn').Pool(min(16, os.cpu_count() or 1)) as pool:
+        days = pool.starmap(synthetic.course_day, [(prof, t, n) for t, n in enumerate(sizes)])
+    return sizes, days
+
+
+def run_chain(args, data):
+    """The large-pair workload: one 60000 x 60000 map in 50-d local PCA on the
+    on-the-fly form, then 20 maps of 20000-60000 cells held as potentials and a
+    pull-back of 8 cell-set indicator vectors through all of them."""
+    import torch
+    import wot_gb300 as wot
+    from wot_gb300 import _build, _native, Population
+    from wot_gb300.ot import device as D
+    from wot_gb300.ot.implicit import ImplicitCoupling
+    from wot_gb300.ot.util import compute_pca
+    import logging
+    logging.disable(logging.WARNING)
+    _build.build()
+    lib = _native.load()
+    sizes, days = data
+    d50 = 50
+    x0, x1, sv, _ = compute_pca(days[0][0], days[1][0], d50)
+    a, b = (x0 * sv).float().contiguous(), (x1 * sv).float().contiguous()
+    G = torch.as_tensor(days[0][1], device='cuda')
+    stream = torch.cuda.current_stream()
+
+    def step():
+        cost = D.default_cost(a, b)
+        res = D.solve(cost, G, CHAIN_CFG, 0, want_tmap=False, want_potentials=True, form='onthefly')
+        return cost, res
+
+    for _ in range(args.warmup):
+        cost, res = step()
+        del cost
+    torch.cuda.synchronize()
+    n_launch0 = lib.wotg_launch_count()
+    with Clocks(0) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        iters = 0
+        for _ in range(args.steps):
+            cost, res = step()
+            iters += res.stats['iterations']
+            if _ < args.steps - 1:
+                del cost
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = lib.wotg_launch_count() - n_launch0
+    t = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    big = ImplicitCoupling.from_solve(cost, res)
+    # FP64 fixed-point residual of the a-update on sampled rows (size-independent
+    # convergence check): ubar_i = eps alpha1 (log p_i - log sum_j dy exp((vbar_j - C_ij)/eps))
+    rng = np.random.default_rng(0)
+    rows = np.sort(rng.choice(sizes[0], 64, replace=False))
+    A64, B64 = a[rows].double(), b.double()
+    C_rows = cost.scale * ((A64[:, None, :] - B64[None, :, :]) ** 2).sum(-1)
+    eps = big.eps
+    a1 = CHAIN_CFG['lambda1'] / (CHAIN_CFG['lambda1'] + eps)
+    lse = torch.logsumexp(-np.log(sizes[1]) + (big.v_bar[None, :] - C_rows) / eps, dim=1)
+    u_fix = eps * a1 * (torch.log(G[rows]) - lse)
+    resid = float((u_fix - big.u_bar[rows]).abs().max() / big.u_bar.abs().max())
+    del cost, C_rows
+
+    # the chain: 20 maps held as potentials
+    chain = []
+    t0 = time.perf_counter()
+    chain_iters = 0
+    chain_elems = 0
+    for k in range(2, len(days) - 1):
+        y0, y1, sk, _ = compute_pca(days[k][0], days[k + 1][0], d50)
+        pa, pb = (y0 * sk).float().contiguous(), (y1 * sk).float().contiguous()
+        c = D.default_cost(pa, pb)
+        r = D.solve(c, torch.as_tensor(days[k][1], device='cuda'), CHAIN_CFG, 0, want_tmap=False,
+                    want_potentials=True, form='onthefly')
+        chain.append(ImplicitCoupling.from_solve(c, r))
+        chain_iters += r.stats['iterations']
+        chain_elems += c.I * c.J
+        del c
+    torch.cuda.synchronize()
+    t_chain = time.perf_counter() - t0
+    tmaps = {(float(k), float(k + 1)): m for k, m in enumerate(chain)}
+    nd = len(chain) + 1
+    ids, dd = [], []
+    for k in range(nd):
+        n = sizes[k + 2]
+        ids += ['d%d_%d' % (k, i) for i in range(n)]
+        dd += [float(k)] * n
+    model = wot.TransportMapModel(tmaps, wot.Frame({'day': np.array(dd)}, index=np.array(ids)))
+    n_last = sizes[-1]
+    P = np.zeros((8, n_last))
+    for k in range(8):
+        P[k, rng.choice(n_last, 500, replace=False)] = 1.0
+    pops = [Population(float(nd - 1), P[k], 'set%d' % k) for k in range(8)]
+    model.pull_back(*pops, to_time=0.0, as_list=True)
+    torch.cuda.synchronize()
+    tp0 = time.perf_counter()
+    back = model.pull_back(*pops, to_time=0.0, as_list=True)
+    torch.cuda.synchronize()
+    t_pull = time.perf_counter() - tp0
+    # reference: the same maps as dense FP64 products, one map at a time on the device
+    ref = torch.as_tensor(P, device='cuda')
+    for m in reversed(chain):
+        T = m.dense()
+        ref = (T @ ref.T).T
+        ref = ref / ref.sum(dim=1, keepdim=True)
+        del T
+    got = torch.as_tensor(np.array([p.p for p in back]), device='cuda')
+    pull_err = float((got - ref).abs().max() / ref.abs().max())
+
+    line = {'metric': METRIC, 'value': 1.0 / t, 'unit': 'maps/s', 'n_gpus': 1, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': t * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': 'large pair %dx%d cells, 50-d local PCA, on-the-fly form (cost tiles recomputed '
+                                   'on the tensor cores), duality-gap solver, eps=0.05 lambda1=1 lambda2=50; then a '
+                                   'chain of %d maps of %d-%d cells held as potentials and a pull-back of 8 indicator '
+                                   'vectors through it' % (sizes[0], sizes[1], len(chain), min(sizes[2:]),
+                                                           max(sizes[2:])),
+                       'I': sizes[0], 'J': sizes[1], 'd': d50,
+                       'timed': 'cost (for the exact median) + median + duality-gap solve, potentials out'},
+            'sinkhorn_iter_per_s': iters / args.steps / t, 'iterations_per_map': iters / args.steps,
+            'element_evaluations_per_s': 2.0 * sizes[0] * sizes[1] * iters / args.steps / t,
+            'fixed_point_residual_sampled_rows': resid,
+            'chain': {'maps': len(chain), 'cells': sizes[2:], 'solve_s': t_chain, 'iterations': chain_iters,
+                      'pull_back_s': t_pull, 'populations': 8,
+                      'pull_back_element_evaluations_per_s': 8.0 * chain_elems / t_pull,
+                      'pull_back_max_rel_err_vs_dense_fp64': pull_err},
+            'gpu_launches': int(launches), 'clocks': clk.summary(), 'e2e': None}
+    print(json.dumps(line), flush=True)
+
 def main():
     global I_FULL, J_FULL, WORKLOAD
     args = parse()
+    if args.workload == 'chain' and args.impl != 'reference':
+        data = chain_days()
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        run_chain(args, data)
+        return
     if args.workload == 'course' and args.impl != 'reference':
         data = course_days(args.course_days)
         import torch

@@ -12,12 +12,13 @@ from __future__ import annotations
 
 import ctypes
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 
 from .. import _native as N
 from . import device as D
+from .implicit import ImplicitCoupling
 
 
 @dataclass
@@ -40,60 +41,19 @@ def prepare_pair(cost: D.DeviceCost, G) -> BatchPair:
     return BatchPair(cost, D.transpose_cost(cost), Gd)
 
 
-@dataclass
-class ImplicitMap:
-    """A transport map as potentials: tmap_ij = exp((u_bar_i + v_bar_j - scale C_ij) / eps) * s,
+class ImplicitMap(ImplicitCoupling):
+    """One batch item's map as potentials: tmap_ij = exp((u_bar_i + v_bar_j - scale C_ij) / eps) * s,
     s = 1/J (or 1 when max_iter was hit), exactly the coupling the reference returns."""
-    pair: BatchPair
-    params: dict
-    u_bar: object
-    v_bar: object
-    row_sums: object
-    learned_growth: list
-    stats: dict
-    status: int
-    eps: float = field(init=False)
-    log_scale: float = field(init=False)
 
-    def __post_init__(self):
-        self.eps = float(self.stats['final_epsilon'])
-        self.log_scale = 0.0 if self.stats['hit_max_iter'] else -math.log(self.pair.cost.J)
-
-    @property
-    def shape(self):
-        return self.pair.shape
-
-    def dense(self):
-        """I x J FP64 device tensor of the coupling."""
-        return D.coupling_from_potentials(self.pair.cost, self.u_bar, self.v_bar, self.eps, self.log_scale)
-
-    def _lse(self, src, tgt_pot, P, C, ldc, rows, cols):
-        torch = N.require_cuda()
-        P = D._dev_f64(P, torch)
-        if P.dim() == 1:
-            P = P.reshape(1, -1)
-        if P.shape[1] != cols:
-            raise ValueError('population length %d does not match %d cells' % (P.shape[1], cols))
-        k = P.shape[0]
-        ldw = N.round_up(cols, 4)
-        W = torch.zeros((k, ldw), dtype=torch.float32, device='cuda')
-        with np.errstate(divide='ignore'):
-            W[:, :cols] = ((tgt_pot / self.eps).reshape(1, -1) + torch.log(P)) * (1.0 / math.log(2.0))
-        kappa2 = self.pair.cost.scale / self.eps / math.log(2.0)
-        L = D.lse_multi(C, rows, cols, ldc, W, [kappa2] * k)
-        return torch.exp(L + (src / self.eps).reshape(1, -1) + self.log_scale)
-
-    def pull_back(self, p, normalize=True):
-        """(tmap @ p.T).T for populations p (k x J): transport_map_model.py:356-358."""
-        c = self.pair.cost
-        out = self._lse(self.u_bar, self.v_bar, p, c.C, c.ldc, c.I, c.J)
-        return out / out.sum(dim=1, keepdim=True) if normalize else out
-
-    def push_forward(self, p, normalize=True):
-        """p @ tmap for populations p (k x I): transport_map_model.py:290-292."""
-        c = self.pair.cost
-        out = self._lse(self.v_bar, self.u_bar, p, self.pair.CT, self.pair.CT.stride(0), c.J, c.I)
-        return out / out.sum(dim=1, keepdim=True) if normalize else out
+    def __init__(self, pair, params, u_bar, v_bar, row_sums, learned_growth, stats, status):
+        c = pair.cost
+        log_scale = 0.0 if stats['hit_max_iter'] else -math.log(c.J)
+        super().__init__(u_bar, v_bar, stats['final_epsilon'], c.scale, log_scale, X=c.X, Y=c.Y, cost=c,
+                         CT=pair.CT, row_sums=row_sums, stats=stats)
+        self.pair = pair
+        self.params = params
+        self.learned_growth = learned_growth
+        self.status = status
 
 
 def solve_batched(pairs, items):

@@ -126,10 +126,19 @@ class TransportMapModel:
         path = find_path(t0, t1, self.day_pairs, self.timepoints)
         return chain_transport_maps(self, path)
 
+    def _implicit(self, t0, t1):
+        """The map t0 -> t1 when it is held as potentials (ImplicitCoupling)."""
+        from ..ot.implicit import ImplicitCoupling
+        m = self.tmaps.get((t0, t1))
+        return m if isinstance(m, ImplicitCoupling) else None
+
     def _device_coupling(self, t0, t1):
         key = (t0, t1)
         if key in self._device:
             return self._device[key]
+        imp = self._implicit(t0, t1)
+        if imp is not None:
+            return imp.dense()
         X = self.get_coupling(t0, t1).X
         torch = N.require_cuda()
         if not (isinstance(X, torch.Tensor) and X.is_cuda and X.dtype == torch.float64):
@@ -158,8 +167,12 @@ class TransportMapModel:
             raise ValueError("Destination timepoint is before source. Unable to push forward")
         p = np.vstack([pop.p for pop in populations])
         while i < j:
-            X = self._device_coupling(self.timepoints[i], self.timepoints[i + 1])
-            p = D.apply_coupling(X, p, transpose=False, normalize=normalize)
+            imp = self._implicit(self.timepoints[i], self.timepoints[i + 1])
+            if imp is not None:
+                p = imp.push_forward(p, normalize=normalize)
+            else:
+                X = self._device_coupling(self.timepoints[i], self.timepoints[i + 1])
+                p = D.apply_coupling(X, p, transpose=False, normalize=normalize)
             i += 1
         p = p.cpu().numpy() if not isinstance(p, np.ndarray) else p
         result = [Population(self.timepoints[i], p[k, :]) for k in range(p.shape[0])]
@@ -181,8 +194,12 @@ class TransportMapModel:
             raise ValueError("Destination timepoint is after source. Unable to pull back")
         p = np.vstack([pop.p for pop in populations])
         while i > j:
-            X = self._device_coupling(self.timepoints[i - 1], self.timepoints[i])
-            p = D.apply_coupling(X, p, transpose=True, normalize=normalize)
+            imp = self._implicit(self.timepoints[i - 1], self.timepoints[i])
+            if imp is not None:
+                p = imp.pull_back(p, normalize=normalize)
+            else:
+                X = self._device_coupling(self.timepoints[i - 1], self.timepoints[i])
+                p = D.apply_coupling(X, p, transpose=True, normalize=normalize)
             i -= 1
         p = p.cpu().numpy() if not isinstance(p, np.ndarray) else p
         result = [Population(self.timepoints[i], p[k, :]) for k in range(p.shape[0])]
