@@ -50,6 +50,8 @@ def parse():
                     help="pair: one 20000x25000 map per step; course: the batched 41-day time course x "
                          "5x5 epsilon/lambda1 sweep (1000 maps) per step")
     ap.add_argument('--course-days', type=int, default=41)
+    ap.add_argument('--no-extra', action='store_true',
+                    help='pair workload only: skip the batched-course and chain summaries of the JSON line')
     ap.add_argument('--form', default='auto', choices=['materialized', 'onthefly', 'auto'],
                     help='materialised FP32 cost stream or tensor-core cost recomputation')
     return ap.parse_args()
@@ -313,7 +315,8 @@ def run_course(args, days_data):
         C = oom.compute_default_cost_matrix(a, b)
         G = days[p][1]
         errs, t_cpu, w_cpu = [], 0.0, 0.0
-        for e, l in ((0.01, 0.1), (0.05, 1), (0.1, 10)):
+        checks = ((0.05, 1), (0.1, 10)) if getattr(args, 'quick', False) else ((0.01, 0.1), (0.05, 1), (0.1, 10))
+        for e, l in checks:
             k = items.index((p, dict(COURSE_CFG, epsilon=e, lambda1=l)))
             st = {}
             t0 = time.perf_counter()
@@ -328,10 +331,11 @@ def run_course(args, days_data):
         line['parity_sample'] = {'pair': p, 'shape': list(C.shape), 'items': errs}
         cpu_value = len(items) / (t_cpu * w_all / w_cpu)
         line['cpu_baseline'] = {'value': cpu_value, 'unit': 'maps/s', 'cores': blas_threads(), 'kind': 'port',
-                                'sample': 'oracle FP64 solves of 3 items of the smallest pair (%dx%d, %.1f s); '
-                                          'extrapolated to all items by sum(iterations * I * J)' % (C.shape[0], C.shape[1], t_cpu)}
+                                'sample': 'oracle FP64 solves of %d items of the smallest pair (%dx%d, %.1f s); '
+                                          'extrapolated to all items by sum(iterations * I * J)'
+                                          % (len(checks), C.shape[0], C.shape[1], t_cpu)}
     line['e2e'] = None
-    print(json.dumps(line), flush=True)
+    return line
 
 
 CHAIN_CFG = dict(growth_iters=1, epsilon=0.05, lambda1=1, lambda2=50, epsilon0=1, tau=10000, scaling_iter=3000,
@@ -472,7 +476,7 @@ def run_chain(args, data):
                       'pull_back_element_evaluations_per_s': 8.0 * chain_elems / t_pull,
                       'pull_back_max_rel_err_vs_dense_fp64': pull_err},
             'gpu_launches': int(launches), 'clocks': clk.summary(), 'e2e': None}
-    print(json.dumps(line), flush=True)
+    return line
 
 def main():
     global I_FULL, J_FULL, WORKLOAD
@@ -481,13 +485,13 @@ def main():
         data = chain_days()
         import torch
         torch.cuda.set_device(dist_env()[2])
-        run_chain(args, data)
+        print(json.dumps(run_chain(args, data)), flush=True)
         return
     if args.workload == 'course' and args.impl != 'reference':
         data = course_days(args.course_days)
         import torch
         torch.cuda.set_device(dist_env()[2])
-        run_course(args, data)
+        print(json.dumps(run_course(args, data)), flush=True)
         return
     if args.pair:
         I_FULL, J_FULL = (int(v) for v in args.pair.split(','))
@@ -495,8 +499,17 @@ def main():
     if args.impl == 'reference':
         run_reference(args)
         return
-    import torch
     rank, world, local = dist_env()
+    extra = rank == 0 and world == 1 and not args.no_extra and args.pair is None
+    course_data = chain_data = None
+    if extra:
+        # day data of the two extra workloads (process pools must start before CUDA)
+        try:
+            course_data = course_days(args.course_days)
+            chain_data = chain_days()
+        except Exception as e:  # noqa: BLE001
+            course_data = chain_data = ('error', repr(e))
+    import torch
     torch.cuda.set_device(local)
     pg = None
     if world > 1:
@@ -650,6 +663,20 @@ def main():
                        'h2d_bytes_per_step': int(X.shape[0] * X.shape[1] * 8 + I_FULL * 8),
                        'd2h_bytes_per_step': int(I_FULL * J_FULL * 8 + 3 * I_FULL * 8),
                        'api': 'wot_gb300.OTModel(Dataset).compute_transport_map(0, 1) (device PCA + cost + solve)'}
+    if extra:
+        # the batched time course (one warm-up, one timed batch) and the large-pair chain
+        sub = argparse.Namespace(**vars(args))
+        sub.steps, sub.warmup, sub.quick = 1, 1, True
+        for key, fn, data in (('course', run_course, course_data), ('chain', run_chain, chain_data)):
+            try:
+                if isinstance(data, tuple) and len(data) == 2 and isinstance(data[0], str):
+                    raise RuntimeError(data[1])
+                r = fn(sub, data)
+                r.pop('metric', None)
+                line[key] = r
+            except Exception as e:  # noqa: BLE001
+                line[key] = {'error': repr(e)}
+            torch.cuda.empty_cache()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg:
