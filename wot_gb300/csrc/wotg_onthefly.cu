@@ -183,14 +183,14 @@ __global__ void tc_bias_pack_kernel(int64_t n, int64_t n_pad, const double* __re
 // Along the walk (cta, tile) only ever steps up, so cta + tile indexes every
 // (CTA, row tile) segment uniquely.
 //
-// Warp roles (18 warps, one CTA per SM):
+// Warp roles (10 warps, two CTAs per SM):
 //   warp 0      producer: bulk asynchronous copies of A tiles (one per segment,
-//               two buffers) and B tiles (a kStages-deep ring);
-//   warp 1      MMA issuer: 6 split-precision MMAs per tile into one of four
-//               128 x 128 FP32 TMEM accumulators; owns the TMEM allocation;
-//   warps 2-17  epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 and the
-//               32 columns of quarter (w - 2) / 4 and folds them into a
-//               running (max, sum).
+//               kABuf buffers) and B tiles (a kStages-deep ring);
+//   warp 1      MMA issuer: 3 split-precision MMAs per 16-column step into one
+//               of two 128 x 128 FP32 TMEM accumulators; owns the TMEM allocation;
+//   warps 2-9   epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 and the
+//               64 columns of half (w - 2) / 4 and folds them into a running
+//               (max, sum).
 // mbarriers hand buffers between roles (full / empty per B stage, per A buffer
 // and per accumulator). Every wait is bounded: a role that times out sets *err
 // and stops; the others then time out in turn, and TMEM is freed at the end.
@@ -207,12 +207,16 @@ template <int KP>
 struct TcSmem {
   static constexpr uint32_t kHalfBytes = 128u * KP * 2u;      // one of hi / lo
   static constexpr uint32_t kTileBytes = 2u * kHalfBytes;      // packed 128-point tile (hi + lo)
-  static constexpr int kStages = KP == 32 ? kTcStages : 1;     // B ring depth (shared-memory budget)
-  static constexpr uint32_t kA = 0;                            // 2 buffers
-  static constexpr uint32_t kB = 2 * kTileBytes;               // kStages buffers
+  // Two CTAs per SM in 96 KB each: 32 columns double-buffer the row tile (A) and
+  // keep a 4-deep ring of column tiles (B); 64 columns single-buffer A (it
+  // changes only at the few row-tile boundaries of a CTA's stretch) and keep 2 B stages.
+  static constexpr int kStages = KP == 32 ? kTcStages : 2;     // B ring depth
+  static constexpr int kABuf = KP == 32 ? 2 : 1;               // A buffers
+  static constexpr uint32_t kA = 0;                            // kABuf buffers
+  static constexpr uint32_t kB = kABuf * kTileBytes;           // kStages buffers
   static constexpr uint32_t kBar = kB + kStages * kTileBytes;
-  // barriers: full[S], empty[S], a_full[2], a_empty[2], acc_full[4], acc_empty[4], TMEM slot
-  static constexpr uint32_t kBytes = kBar + 8 * (2 * kStages + 4 + 2 * kTcAcc) + 16;
+  // barriers: full[S], empty[S], a_full[kABuf], a_empty[kABuf], acc_full[kTcAcc], acc_empty[kTcAcc], TMEM slot
+  static constexpr uint32_t kBytes = kBar + 8 * (2 * kStages + 2 * kABuf + 2 * kTcAcc) + 16;
   static constexpr uint32_t kAlloc = kBytes + 1024;            // slack for 1024-byte alignment
   static constexpr uint32_t kTmemCols = 128 * kTcAcc;
 };
@@ -276,9 +280,10 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
                                                          ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::kBar);
   uint64_t* empty = full + S;
+  constexpr int NA = L::kABuf;
   uint64_t* a_full = empty + S;
-  uint64_t* a_empty = a_full + 2;
-  uint64_t* acc_full = a_empty + 2;
+  uint64_t* a_empty = a_full + NA;
+  uint64_t* acc_full = a_empty + NA;
   uint64_t* acc_empty = acc_full + kTcAcc;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + kTcAcc);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -299,7 +304,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
       tc::mbar_init(&full[b], 1);
       tc::mbar_init(&empty[b], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NA; ++b) {
       tc::mbar_init(&a_full[b], 1);
       tc::mbar_init(&a_empty[b], 1);
     }
@@ -328,13 +333,13 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
         }
         if (j == 0 || q == 0) {
           if (j > 0) ++seg;
-          if (seg >= 2 && !tc::mbar_wait(&a_empty[seg & 1], (uint32_t)(((seg >> 1) - 1) & 1), kTcWaitTries)) {
+          if (seg >= NA && !tc::mbar_wait(&a_empty[seg % NA], (uint32_t)((seg / NA - 1) & 1), kTcWaitTries)) {
             atomicExch(err, 1);
             break;
           }
-          tc::mbar_expect_tx(&a_full[seg & 1], L::kTileBytes);
-          tc::bulk_g2s(sA + (uint32_t)(seg & 1) * L::kTileBytes, Pt + (int64_t)t * tile_halfs, L::kTileBytes,
-                       &a_full[seg & 1]);
+          tc::mbar_expect_tx(&a_full[seg % NA], L::kTileBytes);
+          tc::bulk_g2s(sA + (uint32_t)(seg % NA) * L::kTileBytes, Pt + (int64_t)t * tile_halfs, L::kTileBytes,
+                       &a_full[seg % NA]);
         }
         tc::mbar_expect_tx(&full[stage], L::kTileBytes);
         tc::bulk_g2s(sB + (uint32_t)stage * L::kTileBytes, Qt + (int64_t)q * tile_halfs, L::kTileBytes,
@@ -363,11 +368,11 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
           const int stage = j % S, b = j % kTcAcc;
           const bool new_seg = j == 0 || q == 0;
           if (new_seg && j > 0) ++seg;
-          if (new_seg) good = good && tc::mbar_wait(&a_full[seg & 1], (uint32_t)((seg >> 1) & 1), kTcWaitTries);
+          if (new_seg) good = good && tc::mbar_wait(&a_full[seg % NA], (uint32_t)((seg / NA) & 1), kTcWaitTries);
           good = good && tc::mbar_wait(&full[stage], (uint32_t)((j / S) & 1), kTcWaitTries);
           if (j >= kTcAcc)
             good = good && tc::mbar_wait(&acc_empty[b], (uint32_t)((j / kTcAcc - 1) & 1), kTcWaitTries);
-          a_addr[u] = sA + (uint32_t)(seg & 1) * L::kTileBytes;
+          a_addr[u] = sA + (uint32_t)(seg % NA) * L::kTileBytes;
           b_addr[u] = sB + (uint32_t)stage * L::kTileBytes;
           d_addr[u] = tmem + (uint32_t)(128 * b);
           seg_of[u] = seg;
@@ -399,7 +404,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
           const int j = j0 + u;
           tc::mma_commit(&empty[j % S]);
           tc::mma_commit(&acc_full[j % kTcAcc]);
-          if (seg_end[u]) tc::mma_commit(&a_empty[seg_of[u] & 1]);
+          if (seg_end[u]) tc::mma_commit(&a_empty[seg_of[u] % NA]);
         }
       }
     }
@@ -471,7 +476,10 @@ static cudaError_t tc_set_smem_attr() {
 }
 
 // Resident CTAs per SM of the half-step kernel.
-int tc_ctas_per_sm(int kp) { return kp == 32 ? kTcCtasPerSm : 1; }
+int tc_ctas_per_sm(int kp) {
+  (void)kp;
+  return kTcCtasPerSm;
+}
 int tc_parts() { return kTcParts; }
 
 int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int kp, int ctas, float2* part,
