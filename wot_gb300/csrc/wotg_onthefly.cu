@@ -14,7 +14,7 @@
 
 namespace wotg {
 
-constexpr uint32_t kTcWaitTries = 4096;   // x up to 1 ms per try
+constexpr uint32_t kTcWaitTries = 4000000;  // x up to 1 us per try: about 4 s
 
 // ---------------------------------------------------------------------------
 // Self-test of the MMA path: D (128 x 128, FP32) = A (128 x 32) B (128 x 32)^T
@@ -268,10 +268,28 @@ __device__ __forceinline__ void lse32(const float (&d)[32], float& m, float& s) 
   m = mn;
 }
 
+// Sum of 2^(d[c] - o) of 32 exponents into s (speculative form: o is the row's
+// log-sum-exp from the previous half-step, so no running maximum is needed).
+__device__ __forceinline__ void sum32_off(const float (&d)[32], float o, float& s) {
+  const float2 neg = make_float2(-o, -o);
+  float2 e[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    const float2 z = __fadd2_rn(make_float2(d[2 * c], d[2 * c + 1]), neg);
+    e[c] = make_float2(ex2(z.x), ex2(z.y));
+  }
+#pragma unroll
+  for (int w = 8; w >= 1; w >>= 1)
+#pragma unroll
+    for (int c = 0; c < w; ++c) e[c] = __fadd2_rn(e[c], e[c + w]);
+  s += e[0].x + e[0].y;
+}
+
 template <int KP>
 __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const __half* __restrict__ Pt,
                                                                const __half* __restrict__ Qt,
                                                                int n_pt, int nq, float2* __restrict__ part,
+                                                               const float* __restrict__ off,
                                                                int* __restrict__ err) {
   using L = TcSmem<KP>;
   constexpr int S = L::kStages;
@@ -414,6 +432,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
     const int row = 32 * wq + lane;
     float m = kNegBig, s = 0.f;
     int t = t_first, q = q_first;
+    // speculative form: the row's offset for the current row tile
+    if (off) m = off[(int64_t)t * 128 + row];
     for (int j = 0; j < n; ++j) {
       const int b = j % kTcAcc;
       const bool good =
@@ -423,17 +443,27 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
         break;
       }
       tc::fence_after_sync();
-      float d[kTcColsPerWarp];
-#pragma unroll
-      for (int h = 0; h < kTcColsPerWarp / 32; ++h)
-        tc::tmem_ld32(tmem + ((uint32_t)(32 * wq) << 16) + (uint32_t)(128 * b + kTcColsPerWarp * cq + 32 * h),
-                      *reinterpret_cast<float(*)[32]>(&d[32 * h]));
+      static_assert(kTcColsPerWarp == 64, "two 32-column TMEM blocks per warp and tile");
+      const uint32_t taddr = tmem + ((uint32_t)(32 * wq) << 16) + (uint32_t)(128 * b + kTcColsPerWarp * cq);
+      float d0[32], d1[32];
+      // first block, then the second block's load runs under the first block's sums
+      tc::tmem_ld32(taddr, d0);
       tc::tmem_wait_ld();
+      tc::tmem_hold(d0);
+      tc::tmem_ld32(taddr + 32, d1);
+      if (off)
+        sum32_off(d0, m, s);
+      else
+        lse32(d0, m, s);
+      tc::tmem_wait_ld();
+      tc::tmem_hold(d1);
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
-#pragma unroll
-      for (int h = 0; h < kTcColsPerWarp / 32; ++h) lse32(*reinterpret_cast<float(*)[32]>(&d[32 * h]), m, s);
+      if (off)
+        sum32_off(d1, m, s);
+      else
+        lse32(d1, m, s);
       if (++q == nq || j == n - 1) {
         part[(((int64_t)blockIdx.x + t) * 128 + row) * kTcParts + cq] = make_float2(m, s);
         m = kNegBig;
@@ -442,6 +472,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
           q = 0;
           ++t;
         }
+        if (off && j < n - 1) m = off[(int64_t)t * 128 + row];
       }
     }
   }
@@ -483,13 +514,13 @@ int tc_ctas_per_sm(int kp) {
 int tc_parts() { return kTcParts; }
 
 int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int kp, int ctas, float2* part,
-                  int* err, cudaStream_t st) {
+                  const float* off, int* err, cudaStream_t st) {
   if (kp == 32) {
     WOTG_CUDA(tc_set_smem_attr<32>());
-    lse_tc_kernel<32><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, err);
+    lse_tc_kernel<32><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err);
   } else if (kp == 64) {
     WOTG_CUDA(tc_set_smem_attr<64>());
-    lse_tc_kernel<64><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, err);
+    lse_tc_kernel<64><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err);
   } else {
     return WOTG_BADARG;
   }
@@ -579,7 +610,7 @@ extern "C" int wotg_lse_points(const float* X, int64_t I, int64_t ldx, const flo
   if (s) return s;
   s = tc_pack_bias(J, w, nullptr, P.normY, 1.0, scale * kLog2e, d, P.kp, P.Yb, st);
   if (s) return s;
-  s = tc_lse_launch(P.Xa, P.n_xt, P.Yb, P.n_yt, P.kp, P.ctas, P.part, P.err, st);
+  s = tc_lse_launch(P.Xa, P.n_xt, P.Yb, P.n_yt, P.kp, P.ctas, P.part, nullptr, P.err, st);
   if (s) return s;
   lse_points_finish_kernel<<<(unsigned)((I + 255) / 256), 256, 0, st>>>(I, P.n_yt, P.ctas, kTcParts, P.part,
                                                                         P.normX, scale, L);

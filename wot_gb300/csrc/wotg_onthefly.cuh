@@ -37,7 +37,9 @@ int tc_parts();
 // Persistent launch over n_ptiles x nq tile pairs with `ctas` CTAs; partial of
 // (CTA c, row tile t, row r, column group k) at part[((c + t) * 128 + r) * tc_parts() + k]:
 // (ctas + n_ptiles) * 128 * tc_parts() float2.
+// off (optional, n_ptiles x 128 floats): speculative form, each row's partial
+// is (off_row, sum 2^(d - off_row)); NULL: exact running-maximum form.
 int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int kp, int ctas, float2* part,
-                  int* err, cudaStream_t st);
+                  const float* off, int* err, cudaStream_t st);
 
 }  // namespace wotg

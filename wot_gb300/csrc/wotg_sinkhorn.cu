@@ -81,6 +81,14 @@ struct TcState {
   double* normY;
   float2* part;
   int* err;
+  // Speculative half-steps: each row's base-2 log-sum-exp of the MMA exponents
+  // from the previous half-step (row side offX, column side offY), valid while
+  // epsilon is unchanged; rows whose sum left the safe range are listed in
+  // redo = [count, rows...] and recomputed exactly.
+  float* offX;
+  float* offY;
+  int* redo;
+  bool off_row_ok, off_col_ok;
 };
 
 struct Geom {
@@ -534,10 +542,12 @@ __global__ void __launch_bounds__(256) coupling_kernel(const float* __restrict__
 // (FP32 LSE merge), then the FP64 finish and update.
 template <bool ROW, bool UPDATE>
 __global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restrict__ part, int nq, int ctas,
-                                  int nparts, const double* __restrict__ norm, int parity) {
+                                  int nparts, const double* __restrict__ norm, int parity, int spec,
+                                  float* __restrict__ off, int* __restrict__ redo) {
   const int64_t n = ROW ? g.I : g.J;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double vmax = 0.0;
+  bool skip = false;
   if (i < n) {
     const int64_t t = i >> 7;
     const int64_t total = (((n + 127) >> 7)) * (int64_t)nq;
@@ -551,16 +561,73 @@ __global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restri
         lse_merge(m, s, u.x, u.y);
       }
     }
-    const double L = ((double)m + log2((double)s)) * kLn2 - c.kappa * norm[i];
-    if (ROW) {
-      V.Lrow[i] = L;
-      if (UPDATE) vmax = a_update(i, L, V, c);
+    if (spec && !(s >= 0x1p-80f && s <= 0x1p100f)) {
+      // outside the speculative form's safe range: recomputed exactly
+      const int k = atomicAdd(redo, 1);
+      redo[1 + k] = (int)i;
+      skip = true;
     } else {
-      V.Lcol[i] = L;
-      if (UPDATE) vmax = b_update(i, L, V, c);
+      const double D = (double)m + log2((double)s);
+      off[i] = (float)D;
+      const double L = D * kLn2 - c.kappa * norm[i];
+      if (ROW) {
+        V.Lrow[i] = L;
+        if (UPDATE) vmax = a_update(i, L, V, c);
+      } else {
+        V.Lcol[i] = L;
+        if (UPDATE) vmax = b_update(i, L, V, c);
+      }
     }
   }
+  (void)skip;
   if (UPDATE) block_max_to_slot(vmax, V.maxslot + parity);
+}
+
+// Exact half-step of the rows listed by a speculative combine (a warp per row):
+// L_i = log sum_j exp(w_j - kappa |x_i - y_j|^2) from the FP32 points with a
+// running maximum, then the same update and offset as the combine.
+template <bool ROW, bool UPDATE>
+__global__ void tc_exact_rows_kernel(Geom g, Vecs V, Coef c, const float* __restrict__ P, int64_t ldp,
+                                     const float* __restrict__ Q, int64_t ldq, int d, const double* __restrict__ norm,
+                                     float* __restrict__ off, int* __restrict__ redo, int parity) {
+  const int cnt = redo[0];
+  const int lane = threadIdx.x & 31;
+  const int64_t m_cols = ROW ? g.J : g.I;
+  const double* pot = ROW ? V.v : V.u;
+  const double* lsc = ROW ? V.lb : V.la;
+  const float k2 = (float)(c.kappa * kLog2e);
+  for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < cnt; w += (int)((gridDim.x * blockDim.x) >> 5)) {
+    const int64_t i = redo[1 + w];
+    const float* x = P + i * ldp;
+    float m = kNegBig, s = 0.f;
+    for (int64_t j = lane; j < m_cols; j += 32) {
+      const float* y = Q + j * ldq;
+      float cc = 0.f;
+      for (int t = 0; t < d; ++t) {
+        const float df = x[t] - y[t];
+        cc = fmaf(df, df, cc);
+      }
+      const float tt = (float)((pot[j] * c.inv_eps + lsc[j]) * kLog2e) - k2 * cc;
+      const float mn = fmaxf(m, tt);
+      s = s * ex2(m - mn) + ex2(tt - mn);
+      m = mn;
+    }
+    warp_lse(m, s);
+    if (lane == 0) {
+      const double L2 = (double)m + log2((double)s);
+      off[i] = (float)(L2 + (double)k2 * norm[i]);
+      const double L = L2 * kLn2;
+      double v = 0.0;
+      if (ROW) {
+        V.Lrow[i] = L;
+        if (UPDATE) v = a_update(i, L, V, c);
+      } else {
+        V.Lcol[i] = L;
+        if (UPDATE) v = b_update(i, L, V, c);
+      }
+      if (UPDATE) atomic_max_nonneg(V.maxslot + parity, v);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -588,31 +655,54 @@ struct Solver {
   // (FP16 range); their product is gamma x . y.
   int tc_prepare(const Coef& c) {
     if (!tc.on) return WOTG_OK;
+    tc.off_row_ok = false;  // a new epsilon: the offsets of both sides are stale
+    tc.off_col_ok = false;
     const float gamma = (float)(2.0 * c.kappa * kLog2e / std::sqrt(cost_scale));
     int s = tc_pack_points(tc.X, g.I, tc.ldx, tc.d, tc.kp, gamma, 1, tc.Xa, nullptr, st);
     if (s) return s;
     return tc_pack_points(tc.Y, g.J, tc.ldy, tc.d, tc.kp, gamma, 1, tc.Ya, nullptr, st);
   }
 
+  // The half-steps run in the speculative form once the offsets of their side
+  // exist for the current epsilon (the first half-step of each side after an
+  // epsilon change or a new solve runs the exact form and writes them).
   template <bool UPDATE>
   int tc_row_pass(const Coef& c, int parity) {
     int s = tc_pack_bias(g.J, V.v, V.lb, tc.normY, c.inv_eps, c.kappa * kLog2e, tc.d, tc.kp, tc.Yb, st);
     if (s) return s;
-    s = tc_lse_launch(tc.Xa, tc.n_xt, tc.Yb, tc.n_yt, tc.kp, tc.ctas_row, tc.part, tc.err, st);
+    const bool spec = tc.off_row_ok;
+    if (spec) WOTG_CUDA(cudaMemsetAsync(tc.redo, 0, sizeof(int), st));
+    s = tc_lse_launch(tc.Xa, tc.n_xt, tc.Yb, tc.n_yt, tc.kp, tc.ctas_row, tc.part, spec ? tc.offX : nullptr,
+                      tc.err, st);
     if (s) return s;
-    tc_combine_kernel<true, UPDATE><<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, tc.part, tc.n_yt, tc.ctas_row,
-                                                                          tc_parts(), tc.normX, parity);
+    tc_combine_kernel<true, UPDATE><<<vec_blocks(g.I), 256, 0, st>>>(
+        g, V, c, tc.part, tc.n_yt, tc.ctas_row, tc_parts(), tc.normX, parity, spec ? 1 : 0, tc.offX, tc.redo);
     WOTG_LAUNCHED();
+    if (spec) {
+      tc_exact_rows_kernel<true, UPDATE><<<2 * sm_count(), 256, 0, st>>>(g, V, c, tc.X, tc.ldx, tc.Y, tc.ldy, tc.d,
+                                                                       tc.normX, tc.offX, tc.redo, parity);
+      WOTG_LAUNCHED();
+    }
+    tc.off_row_ok = true;
     return WOTG_OK;
   }
   int tc_col_pass(const Coef& c, int parity) {
     int s = tc_pack_bias(g.I, V.u, V.la, tc.normX, c.inv_eps, c.kappa * kLog2e, tc.d, tc.kp, tc.Xb, st);
     if (s) return s;
-    s = tc_lse_launch(tc.Ya, tc.n_yt, tc.Xb, tc.n_xt, tc.kp, tc.ctas_col, tc.part, tc.err, st);
+    const bool spec = tc.off_col_ok;
+    if (spec) WOTG_CUDA(cudaMemsetAsync(tc.redo, 0, sizeof(int), st));
+    s = tc_lse_launch(tc.Ya, tc.n_yt, tc.Xb, tc.n_xt, tc.kp, tc.ctas_col, tc.part, spec ? tc.offY : nullptr,
+                      tc.err, st);
     if (s) return s;
-    tc_combine_kernel<false, true><<<vec_blocks(g.J), 256, 0, st>>>(g, V, c, tc.part, tc.n_xt, tc.ctas_col,
-                                                                         tc_parts(), tc.normY, parity);
+    tc_combine_kernel<false, true><<<vec_blocks(g.J), 256, 0, st>>>(
+        g, V, c, tc.part, tc.n_xt, tc.ctas_col, tc_parts(), tc.normY, parity, spec ? 1 : 0, tc.offY, tc.redo);
     WOTG_LAUNCHED();
+    if (spec) {
+      tc_exact_rows_kernel<false, true><<<2 * sm_count(), 256, 0, st>>>(g, V, c, tc.Y, tc.ldy, tc.X, tc.ldx, tc.d,
+                                                                      tc.normY, tc.offY, tc.redo, parity);
+      WOTG_LAUNCHED();
+    }
+    tc.off_col_ok = true;
     return WOTG_OK;
   }
 
@@ -976,6 +1066,10 @@ static void tc_layout(Bump& b, const wotg_problem* prob, TcState& tc) {
   tc.part = b.take<float2>((size_t)(std::max(tc.ctas_row, tc.ctas_col) + std::max(tc.n_xt, tc.n_yt)) * 128 *
                            tc_parts());
   tc.err = b.take<int>(4);
+  tc.offX = b.take<float>(tc.I_pad);
+  tc.offY = b.take<float>(tc.J_pad);
+  tc.redo = b.take<int>(2 + std::max(prob->I, prob->J));
+  tc.off_row_ok = tc.off_col_ok = false;
 }
 
 extern "C" size_t wotg_problem_workspace_bytes(const wotg_problem* prob) {

@@ -65,9 +65,9 @@ __device__ __forceinline__ void mbar_fence_init() {
 // Bounded wait for the completion of phase `parity` of an mbarrier. Each
 // try_wait suspends the thread until the phase completes or kSuspendNs
 // nanoseconds pass (so waiting warps sleep instead of polling shared memory);
-// after `max_tries` unsuccessful tries (~max_tries ms) it returns false, so a
+// after `max_tries` unsuccessful tries (~max_tries us) it returns false, so a
 // wait can never hang the kernel.
-constexpr uint32_t kSuspendNs = 1000000;
+constexpr uint32_t kSuspendNs = 1000;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_tries) {
   const uint32_t addr = smem_u32(bar);
   for (uint32_t t = 0; t < max_tries; ++t) {
@@ -116,6 +116,17 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int t = 0; t < 32; ++t) v[t] = __uint_as_float(r[t]);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Ties 32 registers written by tmem_ld32 to the preceding tmem_wait_ld: the
+// compiler sees them redefined here, so no use of them moves above the wait.
+__device__ __forceinline__ void tmem_hold(float (&v)[32]) {
+  asm volatile(""
+               : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7]),
+                 "+f"(v[8]), "+f"(v[9]), "+f"(v[10]), "+f"(v[11]), "+f"(v[12]), "+f"(v[13]), "+f"(v[14]),
+                 "+f"(v[15]), "+f"(v[16]), "+f"(v[17]), "+f"(v[18]), "+f"(v[19]), "+f"(v[20]), "+f"(v[21]),
+                 "+f"(v[22]), "+f"(v[23]), "+f"(v[24]), "+f"(v[25]), "+f"(v[26]), "+f"(v[27]), "+f"(v[28]),
+                 "+f"(v[29]), "+f"(v[30]), "+f"(v[31]));
+}
 
 // Byte offset of element (r, k) in a K-major, no-swizzle tile with K halfs per row.
 __host__ __device__ __forceinline__ uint32_t core_offset(int r, int k, int K) {
