@@ -45,6 +45,7 @@ def parse():
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--pair', default=None, help='I,J cells of a smaller pair (profiling runs)')
+    ap.add_argument('--pca', type=int, default=None, help='local PCA dimension of the pair workload (profiling runs)')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--workload', default='pair', choices=['pair', 'course', 'chain'],
                     help="pair: one 20000x25000 map per step; course: the batched 41-day time course x "
@@ -479,8 +480,11 @@ def run_chain(args, data):
     return line
 
 def main():
-    global I_FULL, J_FULL, WORKLOAD
+    global I_FULL, J_FULL, WORKLOAD, PCA_D
     args = parse()
+    if args.pca:
+        PCA_D = int(args.pca)
+        WORKLOAD = WORKLOAD.replace('local_pca=30', 'local_pca=%d' % PCA_D)
     if args.workload == 'chain' and args.impl != 'reference':
         data = chain_days()
         import torch
@@ -500,7 +504,7 @@ def main():
         run_reference(args)
         return
     rank, world, local = dist_env()
-    extra = rank == 0 and world == 1 and not args.no_extra and args.pair is None
+    extra = rank == 0 and world == 1 and not args.no_extra and args.pair is None and args.pca is None
     course_data = chain_data = None
     if extra:
         # day data of the two extra workloads (process pools must start before CUDA)
