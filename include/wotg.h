@@ -74,7 +74,7 @@ typedef struct wotg_stats {
   double gap;             /* last relative duality gap (duality_gap solver) */
   double final_epsilon;   /* epsilon of the last stage */
   int32_t hit_max_iter;
-  int32_t padding_;
+  int32_t exact_rows;     /* rows the speculative on-the-fly half-step recomputed exactly (diagnostic) */
 } wotg_stats;
 
 /* One transport problem: a dense cost and the source growth G.
@@ -152,9 +152,11 @@ int wotg_compute_transport_matrix(const wotg_problem* problem, const wotg_params
  * absorbed potentials (u_bar, v_bar, device, in/out), n_iter iterations of the
  * reference's a/b updates with tau-absorption at `epsilon`, same problem and
  * workspace as wotg_compute_transport_matrix. Polishes the potentials of a solve
- * stopped on the duality gap towards the exact optimum (before wotg_ot_adjoint). */
+ * stopped on the duality gap towards the exact optimum (before wotg_ot_adjoint).
+ * stats (HOST, may be NULL): iterations = n_iter, absorptions, exact_rows. */
 int wotg_refine_potentials(const wotg_problem* problem, const wotg_params* params, double epsilon, int32_t n_iter,
-                           double* u_bar, double* v_bar, void* workspace, size_t workspace_bytes, void* stream);
+                           double* u_bar, double* v_bar, wotg_stats* stats, void* workspace, size_t workspace_bytes,
+                           void* stream);
 
 /* wotg_compute_transport_matrix for callers that cannot call cudaMalloc (a host
  * whose device memory is owned by another allocator or pool, or a path where

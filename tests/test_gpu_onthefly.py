@@ -104,3 +104,32 @@ def test_lse_points_primitive(I, J, d):
     m = z.max(axis=1)
     ref = m + np.log(np.exp(z - m[:, None]).sum(axis=1))
     np.testing.assert_allclose(L, ref, rtol=0, atol=5e-5 * max(1.0, np.abs(ref).max()))
+
+
+def test_speculative_form_fallback_matches_materialized():
+    """Warm-started iterations from shifted potentials: each side's first
+    half-step runs the exact form, the next ones the speculative form with
+    offsets far from the new sums (a shift of v by s moves a row's
+    log-sum-exp by about (1 - alpha1 alpha2) s / eps per iteration: ~190 in
+    base 2 here), so rows take the exact per-row recompute (exact_rows > 0);
+    the potentials equal the same iterations on the materialised form."""
+    import torch
+    from wot_gb300.ot import device as D
+    cfg = dict(DEFAULTS, lambda1=0.1)
+    x, y, g = _points(700, 900, 30, seed=5)
+    cost = D.default_cost(x, y)
+    res = D.solve(cost, g, cfg, 0, want_tmap=False, want_potentials=True, form='materialized')
+    eps = res.stats['final_epsilon']
+    rng = np.random.default_rng(0)
+    u0 = res.u_bar.clone()
+    v0 = res.v_bar + 20.0 + torch.as_tensor(rng.normal(0.0, 1.0, 900), device='cuda')
+    out = {}
+    for form in ('materialized', 'onthefly'):
+        u, v = u0.clone(), v0.clone()
+        _, _, st = D.refine(cost, g, cfg, u, v, eps, 6, form=form)
+        out[form] = (u.cpu().numpy(), v.cpu().numpy(), st)
+    assert out['onthefly'][2]['exact_rows'] > 0
+    assert out['materialized'][2]['exact_rows'] == 0
+    for k in (0, 1):
+        a, b = out['onthefly'][k], out['materialized'][k]
+        assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max()

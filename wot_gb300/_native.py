@@ -52,10 +52,10 @@ class Params(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [('iterations', ctypes.c_int64), ('absorptions', ctypes.c_int64), ('checks', ctypes.c_int64),
                 ('gap', ctypes.c_double), ('final_epsilon', ctypes.c_double),
-                ('hit_max_iter', ctypes.c_int32), ('padding_', ctypes.c_int32)]
+                ('hit_max_iter', ctypes.c_int32), ('exact_rows', ctypes.c_int32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != 'padding_'}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 FORM_MATERIALIZED = 0
@@ -124,7 +124,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         'wotg_coupling_from_potentials': (ctypes.c_int, [vp, i64, i64, i64, dbl, dbl, vp, vp, dbl, vp, vp]),
         'wotg_ot_adjoint_workspace_bytes': (ctypes.c_size_t, [i64, i64]),
         'wotg_refine_potentials': (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params), dbl, i32, vp, vp,
-                                                  vp, ctypes.c_size_t, vp]),
+                                                  ctypes.POINTER(Stats), vp, ctypes.c_size_t, vp]),
         'wotg_ot_adjoint': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, dbl, dbl, dbl, vp, vp, vp, vp, vp,
                                            vp, ctypes.POINTER(dbl), vp, ctypes.c_size_t, vp]),
         'wotg_lse_matvec_workspace_bytes': (ctypes.c_size_t, [i64, i64, i64]),

@@ -1518,7 +1518,7 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
       o.gap = it.gap;
       o.final_epsilon = it.eps_i;
       o.hit_max_iter = it.hit_max_iter;
-      o.padding_ = 0;
+      o.exact_rows = 0;
     }
     if (statuses) {
       int32_t r = WOTG_OK;

@@ -88,6 +88,7 @@ struct TcState {
   float* offX;
   float* offY;
   int* redo;
+  unsigned long long* redo_total;  // rows recomputed exactly, over the solve (diagnostic)
   bool off_row_ok, off_col_ok;
 };
 
@@ -589,8 +590,10 @@ __global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restri
 template <bool ROW, bool UPDATE>
 __global__ void tc_exact_rows_kernel(Geom g, Vecs V, Coef c, const float* __restrict__ P, int64_t ldp,
                                      const float* __restrict__ Q, int64_t ldq, int d, const double* __restrict__ norm,
-                                     float* __restrict__ off, int* __restrict__ redo, int parity) {
+                                     float* __restrict__ off, int* __restrict__ redo,
+                                     unsigned long long* __restrict__ total, int parity) {
   const int cnt = redo[0];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0) atomicAdd(total, (unsigned long long)cnt);
   const int lane = threadIdx.x & 31;
   const int64_t m_cols = ROW ? g.J : g.I;
   const double* pot = ROW ? V.v : V.u;
@@ -680,7 +683,8 @@ struct Solver {
     WOTG_LAUNCHED();
     if (spec) {
       tc_exact_rows_kernel<true, UPDATE><<<2 * sm_count(), 256, 0, st>>>(g, V, c, tc.X, tc.ldx, tc.Y, tc.ldy, tc.d,
-                                                                       tc.normX, tc.offX, tc.redo, parity);
+                                                                       tc.normX, tc.offX, tc.redo, tc.redo_total,
+                                                                       parity);
       WOTG_LAUNCHED();
     }
     tc.off_row_ok = true;
@@ -699,7 +703,8 @@ struct Solver {
     WOTG_LAUNCHED();
     if (spec) {
       tc_exact_rows_kernel<false, true><<<2 * sm_count(), 256, 0, st>>>(g, V, c, tc.Y, tc.ldy, tc.X, tc.ldx, tc.d,
-                                                                      tc.normY, tc.offY, tc.redo, parity);
+                                                                      tc.normY, tc.offY, tc.redo, tc.redo_total,
+                                                                      parity);
       WOTG_LAUNCHED();
     }
     tc.off_col_ok = true;
@@ -1069,6 +1074,7 @@ static void tc_layout(Bump& b, const wotg_problem* prob, TcState& tc) {
   tc.offX = b.take<float>(tc.I_pad);
   tc.offY = b.take<float>(tc.J_pad);
   tc.redo = b.take<int>(2 + std::max(prob->I, prob->J));
+  tc.redo_total = b.take<unsigned long long>(1);
   tc.off_row_ok = tc.off_col_ok = false;
 }
 
@@ -1128,6 +1134,7 @@ extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wot
   if (tc_requested(prob)) {
     tc_layout(b, prob, S.tc);
     WOTG_CUDA(cudaMemsetAsync(S.tc.err, 0, sizeof(int), st));
+    WOTG_CUDA(cudaMemsetAsync(S.tc.redo_total, 0, sizeof(unsigned long long), st));
     // column forms (coordinates; bias columns written per half-step) and norms
     const float sigma = (float)std::sqrt(prob->cost_scale);
     int s = tc_pack_points(prob->X, I, prob->ldx, prob->d, S.tc.kp, sigma, 0, S.tc.Xb, S.tc.normX, st);
@@ -1187,6 +1194,9 @@ extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wot
       set_last_message("tensor-core half-step: a bounded wait timed out");
       return WOTG_CUDA_ERROR;
     }
+    unsigned long long redo = 0;
+    WOTG_CUDA(cudaMemcpy(&redo, S.tc.redo_total, sizeof(redo), cudaMemcpyDeviceToHost));
+    total.exact_rows = (int32_t)std::min<unsigned long long>(redo, 0x7fffffffull);
   }
   if (stats) *stats = total;
   return status;
@@ -1199,8 +1209,8 @@ extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wot
 // Polishes a solve stopped on the duality gap towards the exact optimum (used
 // before differentiating the objective).
 extern "C" int wotg_refine_potentials(const wotg_problem* prob, const wotg_params* params, double epsilon,
-                                      int32_t n_iter, double* u_bar, double* v_bar, void* workspace,
-                                      size_t workspace_bytes, void* stream) {
+                                      int32_t n_iter, double* u_bar, double* v_bar, wotg_stats* stats,
+                                      void* workspace, size_t workspace_bytes, void* stream) {
   if (!prob || !params || !u_bar || !v_bar || n_iter < 0 || !(epsilon > 0)) return WOTG_BADARG;
   const wotg_params P = *params;
   const int64_t I = prob->I, J = prob->J, ldc = prob->ldc;
@@ -1218,6 +1228,7 @@ extern "C" int wotg_refine_potentials(const wotg_problem* prob, const wotg_param
   if (tc_requested(prob)) {
     tc_layout(b, prob, S.tc);
     WOTG_CUDA(cudaMemsetAsync(S.tc.err, 0, sizeof(int), st));
+    WOTG_CUDA(cudaMemsetAsync(S.tc.redo_total, 0, sizeof(unsigned long long), st));
     const float sigma = (float)std::sqrt(prob->cost_scale);
     int s = tc_pack_points(prob->X, I, prob->ldx, prob->d, S.tc.kp, sigma, 0, S.tc.Xb, S.tc.normX, st);
     if (s) return s;
@@ -1245,6 +1256,15 @@ extern "C" int wotg_refine_potentials(const wotg_problem* prob, const wotg_param
   s = S.outputs(c, false, nullptr, nullptr, u_bar, v_bar);
   if (s) return s;
   WOTG_CUDA(cudaStreamSynchronize(st));
+  wotg_stats out{};
+  out.iterations = n_iter;
+  out.final_epsilon = epsilon;
+  out.gap = NAN;
+  {
+    int absorptions = 0;
+    WOTG_CUDA(cudaMemcpy(&absorptions, V.counters, sizeof(int), cudaMemcpyDeviceToHost));
+    out.absorptions = absorptions;
+  }
   if (S.tc.on) {
     int err = 0;
     WOTG_CUDA(cudaMemcpy(&err, S.tc.err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1252,7 +1272,11 @@ extern "C" int wotg_refine_potentials(const wotg_problem* prob, const wotg_param
       set_last_message("tensor-core half-step: a bounded wait timed out");
       return WOTG_CUDA_ERROR;
     }
+    unsigned long long redo = 0;
+    WOTG_CUDA(cudaMemcpy(&redo, S.tc.redo_total, sizeof(redo), cudaMemcpyDeviceToHost));
+    out.exact_rows = (int32_t)std::min<unsigned long long>(redo, 0x7fffffffull);
   }
+  if (stats) *stats = out;
   return WOTG_OK;
 }
 

@@ -41,7 +41,7 @@ def _function():
             eps = res.stats['final_epsilon']
             u, v = res.u_bar, res.v_bar
             if refine_iters > 0:
-                D.refine(cost, p, cfg, u, v, eps, refine_iters, form=form)
+                D.refine(cost, p, cfg, u, v, eps, refine_iters, form=form)  # in place
             obj, gx, gy, gp = D.ot_adjoint(X, Y, cost.scale, eps, cfg['lambda1'], cfg['lambda2'], u, v, p)
             ctx.save_for_backward(gx, gy, gp * p * dt)
             ctx.dtypes = (x.dtype, y.dtype, log_g.dtype, x.device, y.device, log_g.device, log_g.shape)

@@ -209,10 +209,11 @@ def refine(cost: DeviceCost, G, cfg: dict, u_bar, v_bar, eps: float, n_iter: int
     prob = _problem(cost, Gd, form)
     nbytes = lib.wotg_problem_workspace_bytes(ctypes.byref(prob))
     ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
+    stats = N.Stats()
     N.check(lib.wotg_refine_potentials(ctypes.byref(prob), ctypes.byref(params), float(eps), int(n_iter),
-                                       u_bar.data_ptr(), v_bar.data_ptr(), ws.data_ptr(), nbytes, _stream()),
-            'wotg_refine_potentials')
-    return u_bar, v_bar
+                                       u_bar.data_ptr(), v_bar.data_ptr(), ctypes.byref(stats), ws.data_ptr(),
+                                       nbytes, _stream()), 'wotg_refine_potentials')
+    return u_bar, v_bar, stats.as_dict()
 
 
 def ot_adjoint(X, Y, cost_scale: float, eps: float, lambda1: float, lambda2: float, u_bar, v_bar, p,
