@@ -79,7 +79,12 @@ class Dataset:
             rows, cols = key, slice(None)
         r = _rows(rows, self.shape[0])
         c = _rows(cols, self.shape[1])
-        X = self.X[r][:, c] if self.X is not None else None
+        if self.X is None:
+            X = None
+        else:
+            # slices index X as views (no copy of the expression matrix)
+            X = self.X[rows if isinstance(rows, slice) else r]
+            X = X[:, cols] if isinstance(cols, slice) else X[:, c]
         return Dataset(X, self.obs[r], self.var[c])
 
     def copy(self):

@@ -215,7 +215,7 @@ class OTModel:
             cv = ds_.column(obs, self.covariate_field)
             s0 = (day == float(t0)) & (cv == covariate[0])
             s1 = (day == float(t1)) & (cv == covariate[1])
-        return self.matrix[s0, :], self.matrix[s1, :]
+        return self.matrix[_as_slice(s0), :], self.matrix[_as_slice(s1), :]
 
     def compute_single_transport_map(self, config):
         """One transport map (ot_model.py:255-326)."""
@@ -250,13 +250,56 @@ class OTModel:
             config['G'] = np.ones(n0)
         sid = ot.native_solver_id(self.solver)
         cost = C if isinstance(C, D.DeviceCost) else D.cost_from_dense(C)
+        # the host array of the FP64 map is allocated and its pages faulted in on
+        # host threads while the GPU works; the copy into it then runs at link speed
+        out = _prefaulted_async(C.shape[0], C.shape[1])
         res = D.solve(cost, config['G'], config, sid, want_tmap=True, form=self.form)
-        tmap = res.tmap.cpu().numpy()
+        tmap = out.result()
+        N.require_cuda().from_numpy(tmap).copy_(res.tmap)
         learned = [np.asarray(config['G'], dtype=np.float64)] + [g.cpu().numpy() for g in res.learned_growth[1:]]
         learned.append(res.row_sums.cpu().numpy())
         obs_growth = {'g' + str(i): np.power(g, 1.0 / delta_days) for i, g in enumerate(learned)}
         self.last_stats = res.stats
         return ds_.make_result(tmap, obs_growth, ds_.index(p0.obs), ds_.index(p1.obs), like=self.matrix)
+
+
+def _as_slice(mask):
+    """A boolean row mask as a slice when its rows are contiguous (a view of the
+    matrix instead of a copy), else the mask."""
+    idx = np.flatnonzero(mask)
+    if idx.size and idx[-1] - idx[0] + 1 == idx.size:
+        return slice(int(idx[0]), int(idx[-1]) + 1)
+    return mask
+
+
+_TOUCH_POOL = None
+
+
+def _prefaulted_async(rows, cols, parts=8):
+    """Future of an uninitialised (rows x cols) FP64 array whose pages have been
+    written once (one store per 4 KB, spread over host threads), so that a
+    device-to-host copy into it does not stop on first-touch page faults."""
+    from concurrent.futures import ThreadPoolExecutor
+    global _TOUCH_POOL
+    if _TOUCH_POOL is None:
+        _TOUCH_POOL = ThreadPoolExecutor(max_workers=parts, thread_name_prefix='wotg-prefault')
+    arr = np.empty((int(rows), int(cols)), dtype=np.float64)
+    flat = arr.reshape(-1)
+    step = 512  # 4 KB of float64
+    bounds = np.linspace(0, flat.size, parts + 1).astype(np.int64)
+
+    def touch(a, b):
+        flat[a:b:step] = 0.0
+
+    futs = [_TOUCH_POOL.submit(touch, int(bounds[k]), int(bounds[k + 1])) for k in range(parts)]
+
+    class _Result:
+        def result(self):
+            for f in futs:
+                f.result()
+            return arr
+
+    return _Result()
 
 
 def _filter(adata, cell_filter, gene_filter):
