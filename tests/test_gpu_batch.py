@@ -175,3 +175,22 @@ def test_implicit_map_pull_back_push_forward():
     ref_push = pi @ T
     assert np.abs(pull - ref_pull).max() <= 1e-5 * np.abs(ref_pull).max()
     assert np.abs(push - ref_push).max() <= 1e-5 * np.abs(ref_push).max()
+
+
+def test_otmodel_batched_sweep_matches_single_maps():
+    """OTModel.compute_transport_maps_batched on a 3-day course x 2 parameter
+    sets: every map equals OTModel.compute_transport_map with that parameter set."""
+    import wot_gb300 as wot
+    from wot_gb300 import synthetic
+    X, day, growth = synthetic.time_course([300, 350, 280], n_genes=200, n_clusters=4, seed=3)
+    ids = np.array(['c%d' % i for i in range(len(day))])
+    ds = wot.Dataset(X, wot.Frame({'day': day, 'cell_growth_rate': growth}, index=ids))
+    model = wot.OTModel(ds, local_pca=20, form='materialized')
+    sweep = [{'epsilon': 0.05, 'lambda1': 1.0}, {'epsilon': 0.1, 'lambda1': 3.0}]
+    maps = model.compute_transport_maps_batched(sweep=sweep)
+    assert sorted(maps) == [(0.0, 1.0, 0), (0.0, 1.0, 1), (1.0, 2.0, 0), (1.0, 2.0, 1)]
+    for (t0, t1, i), m in maps.items():
+        ref = wot.OTModel(ds, local_pca=20, form='materialized', **sweep[i]).compute_transport_map(t0, t1)
+        R = np.asarray(ref.X)
+        T = m.dense().cpu().numpy()
+        assert coupling_err(T, R) <= SAME_DEVICE_TOL

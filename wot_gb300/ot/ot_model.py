@@ -174,6 +174,52 @@ class OTModel:
         if learned_tables:
             write_learned_growth(learned_tables, os.path.join(tmap_dir, tmap_prefix + '_g.txt'))
 
+    def compute_transport_maps_batched(self, day_pairs=None, sweep=None):
+        """Every day pair (the consecutive days, or ``day_pairs``) for every
+        parameter set of ``sweep`` (a list of ot_config overrides, e.g.
+        ``[{'epsilon': e, 'lambda1': l} for e in ... for l in ...]``; default:
+        the model's own configuration) in one batched solve (no counterpart in
+        the reference, which solves them one by one, ot_model.py:124-201).
+
+        Each pair's cost is built on the device as compute_single_transport_map
+        does (day selection, local PCA, median-normalised cost, G = g^(t1 - t0));
+        the solver is the duality-gap one. Returns a dict
+        {(t0, t1, i): ImplicitMap} with i the index into ``sweep``; an
+        ImplicitMap holds the map as potentials (``.dense()``, ``.pull_back``,
+        ``.push_forward``, ``.row_sums``, ``.stats``)."""
+        from . import batch as B
+        if self.solver is not ot.optimal_transport_duality_gap:
+            raise ValueError('batched solves use the duality-gap solver')
+        t = self.timepoints
+        pairs_days = list(day_pairs) if day_pairs else [(t[i], t[i + 1]) for i in range(len(t) - 1)]
+        sweep = list(sweep) if sweep else [{}]
+        pairs, keys = [], []
+        for t0, t1 in pairs_days:
+            config = {**self.ot_config, 't0': t0, 't1': t1, 'covariate': None}
+            p0, p1 = self.select_pair(config)
+            if p0.shape[0] == 0 or p1.shape[0] == 0:
+                continue
+            local_pca = config.get('local_pca')
+            if local_pca is not None and local_pca > 0:
+                x0, x1, sv, _ = compute_pca(p0.X, p1.X, local_pca)
+                cost = OTModel.compute_default_cost_matrix(x0, x1, sv)
+            else:
+                cost = OTModel.compute_default_cost_matrix(p0.X, p1.X)
+            delta = t1 - t0
+            if self.cell_growth_rate_field in ds_.columns(p0.obs):
+                G = np.power(ds_.column(p0.obs, self.cell_growth_rate_field).astype(np.float64), delta)
+            else:
+                G = np.ones(p0.shape[0])
+            pairs.append(B.prepare_pair(cost, G))
+            keys.append((t0, t1))
+        items, names = [], []
+        for p, (t0, t1) in enumerate(keys):
+            for i, over in enumerate(sweep):
+                items.append((p, {**self.ot_config, **over}))
+                names.append((t0, t1, i))
+        maps = B.solve_batched(pairs, items)
+        return dict(zip(names, maps))
+
     def compute_transport_map(self, t0, t1, covariate=None, cost_matrix=None):
         """Transport map from t0 to t1 (ot_model.py:203-240)."""
         if self.day_pairs is not None:
