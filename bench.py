@@ -62,6 +62,18 @@ def dist_env():
     return int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)), int(os.environ.get('LOCAL_RANK', 0))
 
 
+def exp2_peak():
+    """Measured exp2 throughput of this GPU (the half-steps' per-element ceiling)."""
+    import ctypes
+    import torch
+    from wot_gb300 import _native
+    r = ctypes.c_double(0.0)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if _native.load().wotg_exp2_rate(ctypes.byref(r), st) != 0:
+        return None
+    return r.value
+
+
 def peaks():
     """(HBM GB/s, dense bf16 TFLOP/s, 'measured' | 'fallback')."""
     try:
@@ -297,6 +309,7 @@ def run_course(args, days_data):
             'sinkhorn_iter_per_s': float(np.sum(its)) / t, 'iterations_per_map': float(np.mean(its)),
             'max_iterations': int(its.max()),
             'element_evaluations_per_s': work / t,
+            'exp2_peak_per_s': exp2_peak(),
             'batched_vs_plain': {
                 'subset_pairs': subset, 'subset_items': len(sub_items),
                 'batched_s': t_sub_batched, 'plain_auto_s': t_plain['auto'],
@@ -309,7 +322,7 @@ def run_course(args, days_data):
                         'by sum(iterations * I * J)'},
             'gpu_launches': int(launches), 'clocks': clk.summary(), 'peaks': {'kind': peak_kind}}
     if not args.no_cpu:
-        # parity and CPU baseline: the oracle on three items of the smallest pair
+        # parity and CPU baseline: the oracle on items of the smallest pair
         from oracle import ot_model as oom, optimal_transport as oot
         p = int(order[0])
         a, b = (x.double().cpu().numpy() for x in pts[p])
@@ -579,6 +592,7 @@ def main():
         return float(np.mean([evs[2 * r].elapsed_time(evs[2 * r + 1]) for r in range(reps)])) / 1e3
 
     hbm_peak, tf_peak, peak_kind = peaks()
+    exp_pk = exp2_peak()
     # materialised form: streaming row pass over the FP32 cost (HBM-bound)
     ldc = cost.ldc
     w = torch.zeros(ldc, dtype=torch.float32, device='cuda')
@@ -613,6 +627,8 @@ def main():
                'kernel': 'lse_tc_kernel (wotg_lse_points)', 'peak_kind': peak_kind, 'launch_ms': t_tc * 1e3,
                'executed_mma_tflops': 3 * 2.0 * 32 * I_FULL * J_FULL / t_tc / 1e12,
                'exp_per_s': I_FULL * J_FULL / t_tc,
+               'exp2_peak_per_s': exp_pk,
+               'exp2_frac': (I_FULL * J_FULL / t_tc / exp_pk) if exp_pk else None,
                'note': 'the exp + FP32 reduction of every cost element (one per element, from TMEM) bounds this '
                        'kernel, not the split-precision MMA (3 FP16 products per contraction step)'}
     roofline = roof_tc if form == _native.FORM_ONTHEFLY else roof_mat

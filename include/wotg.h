@@ -309,6 +309,12 @@ int wotg_ot_adjoint(const float* X, int64_t I, int64_t ldx, const float* Y, int6
                     const double* v_bar, const double* p, double* grad_x, double* grad_y, double* grad_p,
                     double* objective, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Diagnostic (no counterpart in the reference): this GPU's measured throughput
+ * of ex2.approx.ftz.f32 (exp2 per second, a register-only kernel timed with CUDA
+ * events on `stream`, best of 3). Every half-step form spends one exp2 per cost
+ * element, so this is their ceiling; allocates nothing; synchronises the stream. */
+int wotg_exp2_rate(double* exp2_per_s, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

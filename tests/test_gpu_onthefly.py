@@ -133,3 +133,15 @@ def test_speculative_form_fallback_matches_materialized():
     for k in (0, 1):
         a, b = out['onthefly'][k], out['materialized'][k]
         assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max()
+
+
+def test_exp2_rate_is_measured():
+    """wotg_exp2_rate: the measured ex2 throughput, the per-element ceiling of every
+    half-step form, lies between 1e12 and 1e14 exp2/s on this part."""
+    import ctypes
+    import torch
+    from wot_gb300 import _native
+    r = ctypes.c_double(0.0)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert _native.load().wotg_exp2_rate(ctypes.byref(r), st) == 0
+    assert 1e12 < r.value < 1e14
