@@ -618,13 +618,30 @@ def main():
     wj = torch.zeros(J_FULL, dtype=torch.float64, device='cuda')
     wsp = torch.empty(lib.wotg_lse_points_workspace_bytes(I_FULL, J_FULL, PCA_D), dtype=torch.uint8, device='cuda')
     sc = float(cost.scale / CFG['epsilon'])
-    t_tc = time_launches(lambda: lib.wotg_lse_points(a.data_ptr(), I_FULL, a.stride(0), b.data_ptr(), J_FULL,
-                                                     b.stride(0), PCA_D, sc, wj.data_ptr(), L.data_ptr(),
-                                                     wsp.data_ptr(), wsp.numel(), sh))
+
+    def tc_kernel_s(speculative):
+        # the tensor-core kernel alone, 20 launches timed with CUDA events on this stream
+        r = ctypes.c_float(0.0)
+        _native.check(lib.wotg_lse_points_timing(a.data_ptr(), I_FULL, a.stride(0), b.data_ptr(), J_FULL,
+                                                 b.stride(0), PCA_D, sc, wj.data_ptr(), speculative, reps,
+                                                 ctypes.byref(r), wsp.data_ptr(), wsp.numel(), sh),
+                      'wotg_lse_points_timing')
+        return r.value * 1e-3
+
+    t_tc = tc_kernel_s(1)        # the form the solve runs once a row's previous LSE is known
+    t_tc_exact = tc_kernel_s(0)  # the form of the first half-step after each epsilon change
+    t_tc_call = time_launches(lambda: lib.wotg_lse_points(a.data_ptr(), I_FULL, a.stride(0), b.data_ptr(), J_FULL,
+                                                          b.stride(0), PCA_D, sc, wj.data_ptr(), L.data_ptr(),
+                                                          wsp.data_ptr(), wsp.numel(), sh))
     flops = 2.0 * PCA_D * I_FULL * J_FULL           # algorithmic cross-term contraction
+    # DRAM bytes per launch from an ncu capture of this kernel inside this workload's solve
+    # (5.89e6 and 5.93e6 B read, 0 written): the packed FP16 hi/lo points, read once
+    tc_traffic = (5893888 + 5927168) / 2 / (20000 + 25000) * (I_FULL + J_FULL)
     roof_tc = {'bound': 'tensor', 'achieved': flops / t_tc / 1e12, 'peak': tf_peak, 'unit': 'TFLOP/s',
-               'frac': flops / t_tc / 1e12 / tf_peak, 'traffic': None,
-               'kernel': 'lse_tc_kernel (wotg_lse_points)', 'peak_kind': peak_kind, 'launch_ms': t_tc * 1e3,
+               'frac': flops / t_tc / 1e12 / tf_peak, 'traffic': tc_traffic,
+               'kernel': 'lse_tc_kernel<32> (speculative form, as in the solve)', 'peak_kind': peak_kind,
+               'launch_ms': t_tc * 1e3, 'exact_form_launch_ms': t_tc_exact * 1e3,
+               'wotg_lse_points_call_ms': t_tc_call * 1e3,
                'executed_mma_tflops': 3 * 2.0 * 32 * I_FULL * J_FULL / t_tc / 1e12,
                'exp_per_s': I_FULL * J_FULL / t_tc,
                'exp2_peak_per_s': exp_pk,

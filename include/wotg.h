@@ -195,6 +195,17 @@ int wotg_lse_points(const float* X, int64_t I, int64_t ldx, const float* Y, int6
                     double scale, const double* w, double* L, void* workspace, size_t workspace_bytes,
                     void* stream);
 
+/* Diagnostic (no counterpart in the reference): the mean device time of the
+ * tensor-core kernel of wotg_lse_points alone (no packing, no finish), over
+ * n_launch back-to-back launches timed with CUDA events on `stream`. With
+ * speculative != 0 each launch runs the form the solver uses once a row's
+ * previous log-sum-exp is known (sums taken against that offset, no running
+ * maximum); the offsets come from one exact launch first. Same arguments and
+ * workspace as wotg_lse_points; synchronises the stream. */
+int wotg_lse_points_timing(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy,
+                           int32_t d, double scale, const double* w, int32_t speculative, int32_t n_launch,
+                           float* ms_per_launch, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Diagnostics (no counterpart in the reference): one 128 x 128 x 32 tensor-core
  * product D = A B^T through the FP16 split used by the on-the-fly form
  * (terms = 1: hi.hi; 3: hi.hi + hi.lo + lo.hi), with the shared-memory

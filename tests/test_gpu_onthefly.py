@@ -145,3 +145,27 @@ def test_exp2_rate_is_measured():
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     assert _native.load().wotg_exp2_rate(ctypes.byref(r), st) == 0
     assert 1e12 < r.value < 1e14
+
+
+def test_lse_points_kernel_timing():
+    """wotg_lse_points_timing: both forms of the tensor-core kernel run and time
+    positive; the speculative form (sums against the previous log-sum-exp) is no
+    slower than the exact form with its running maximum (10 % allowance)."""
+    import ctypes
+    import torch
+    from wot_gb300 import _native, synthetic
+    lib = _native.load()
+    I, J, d = 3000, 3500, 30
+    X = torch.tensor(synthetic.gaussian_mixture_points(I, d=d, seed=3), dtype=torch.float32, device='cuda')
+    Y = torch.tensor(synthetic.gaussian_mixture_points(J, d=d, seed=4), dtype=torch.float32, device='cuda')
+    w = torch.zeros(J, dtype=torch.float64, device='cuda')
+    ws = torch.empty(lib.wotg_lse_points_workspace_bytes(I, J, d), dtype=torch.uint8, device='cuda')
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ms = {}
+    for spec in (0, 1):
+        r = ctypes.c_float(0.0)
+        assert lib.wotg_lse_points_timing(X.data_ptr(), I, d, Y.data_ptr(), J, d, d, 0.05, w.data_ptr(), spec, 10,
+                                          ctypes.byref(r), ws.data_ptr(), ws.numel(), st) == 0
+        ms[spec] = r.value
+    assert ms[0] > 0 and ms[1] > 0
+    assert ms[1] <= 1.1 * ms[0]

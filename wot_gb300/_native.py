@@ -37,7 +37,7 @@ EXPORTS = (
     'wotg_lse_points_workspace_bytes', 'wotg_lse_points', 'wotg_transpose_cost', 'wotg_batch_workspace_bytes',
     'wotg_solve_batched', 'wotg_lse_matvec_multi_workspace_bytes', 'wotg_lse_matvec_multi',
     'wotg_coupling_from_potentials', 'wotg_ot_adjoint_workspace_bytes', 'wotg_ot_adjoint',
-    'wotg_refine_potentials', 'wotg_exp2_rate',
+    'wotg_refine_potentials', 'wotg_exp2_rate', 'wotg_lse_points_timing',
 )
 
 
@@ -124,6 +124,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         'wotg_coupling_from_potentials': (ctypes.c_int, [vp, i64, i64, i64, dbl, dbl, vp, vp, dbl, vp, vp]),
         'wotg_ot_adjoint_workspace_bytes': (ctypes.c_size_t, [i64, i64]),
         'wotg_exp2_rate': (ctypes.c_int, [ctypes.POINTER(dbl), vp]),
+        'wotg_lse_points_timing': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, vp, i32, i32,
+                                                  ctypes.POINTER(ctypes.c_float), vp, ctypes.c_size_t, vp]),
         'wotg_refine_potentials': (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params), dbl, i32, vp, vp,
                                                   ctypes.POINTER(Stats), vp, ctypes.c_size_t, vp]),
         'wotg_ot_adjoint': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, dbl, dbl, dbl, vp, vp, vp, vp, vp,

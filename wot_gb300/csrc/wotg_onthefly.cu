@@ -529,9 +529,11 @@ int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int 
 }
 
 
-// Finish of the standalone half-step: L_i = ln2 (m + log2 s) - scale |x_i|^2.
+// Finish of the standalone half-step: L_i = ln2 (m + log2 s) - scale |x_i|^2; with
+// `off`, also the base-2 offset m + log2 s that the speculative form reads.
 __global__ void lse_points_finish_kernel(int64_t n, int nq, int ctas, int nparts, const float2* __restrict__ part,
-                                         const double* __restrict__ norm, double scale, double* __restrict__ L) {
+                                         const double* __restrict__ norm, double scale, double* __restrict__ L,
+                                         float* __restrict__ off) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int64_t t = i >> 7;
@@ -543,7 +545,9 @@ __global__ void lse_points_finish_kernel(int64_t n, int nq, int ctas, int nparts
     const float2* pp = part + ((cc + t) * 128 + (i & 127)) * nparts;
     for (int k = 0; k < nparts; ++k) lse_merge(m, s, pp[k].x, pp[k].y);
   }
-  L[i] = ((double)m + log2((double)s)) * kLn2 - scale * norm[i];
+  const double D = (double)m + log2((double)s);
+  if (L) L[i] = D * kLn2 - scale * norm[i];
+  if (off) off[i] = (float)D;
 }
 
 struct PointsLayout {
@@ -553,6 +557,7 @@ struct PointsLayout {
   double* normX;
   double* normY;
   float2* part;
+  float* off;
   int* err;
 };
 
@@ -567,6 +572,7 @@ static size_t points_layout(Bump& b, int64_t I, int64_t J, int d, PointsLayout& 
   P.normX = b.take<double>(I);
   P.normY = b.take<double>(J);
   P.part = b.take<float2>((size_t)(P.ctas + P.n_xt) * 128 * kTcParts);
+  P.off = b.take<float>((size_t)P.n_xt * 128);
   P.err = b.take<int>(4);
   return b.off + 256;
 }
@@ -613,7 +619,65 @@ extern "C" int wotg_lse_points(const float* X, int64_t I, int64_t ldx, const flo
   s = tc_lse_launch(P.Xa, P.n_xt, P.Yb, P.n_yt, P.kp, P.ctas, P.part, nullptr, P.err, st);
   if (s) return s;
   lse_points_finish_kernel<<<(unsigned)((I + 255) / 256), 256, 0, st>>>(I, P.n_yt, P.ctas, kTcParts, P.part,
-                                                                        P.normX, scale, L);
+                                                                        P.normX, scale, L, nullptr);
   WOTG_LAUNCHED();
+  return WOTG_OK;
+}
+
+extern "C" int wotg_lse_points_timing(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J,
+                                      int64_t ldy, int32_t d, double scale, const double* w, int32_t speculative,
+                                      int32_t n_launch, float* ms_per_launch, void* workspace,
+                                      size_t workspace_bytes, void* stream) {
+  if (!X || !Y || !w || !ms_per_launch || I <= 0 || J <= 0 || d < 1 || d > tc_max_dim() || ldx < d ||
+      ldy < d || !(scale > 0) || n_launch < 1 || n_launch > 10000)
+    return WOTG_BADARG;
+  if (!workspace || workspace_bytes < wotg_lse_points_workspace_bytes(I, J, d)) return WOTG_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  Bump b{reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255)), 0};
+  PointsLayout P{};
+  points_layout(b, I, J, d, P);
+  const double sigma = std::sqrt(scale);
+  WOTG_CUDA(cudaMemsetAsync(P.err, 0, sizeof(int), st));
+  WOTG_CUDA(cudaMemsetAsync(P.off, 0, sizeof(float) * (size_t)P.n_xt * 128, st));
+  int s = tc_pack_points(X, I, ldx, d, P.kp, (float)(2.0 * kLog2e * sigma), 1, P.Xa, P.normX, st);
+  if (s) return s;
+  s = tc_pack_points(Y, J, ldy, d, P.kp, (float)sigma, 0, P.Yb, P.normY, st);
+  if (s) return s;
+  s = tc_pack_bias(J, w, nullptr, P.normY, 1.0, scale * kLog2e, d, P.kp, P.Yb, st);
+  if (s) return s;
+  // one exact launch gives every row's offset (the previous LSE, as in the solve's steady state)
+  s = tc_lse_launch(P.Xa, P.n_xt, P.Yb, P.n_yt, P.kp, P.ctas, P.part, nullptr, P.err, st);
+  if (s) return s;
+  lse_points_finish_kernel<<<(unsigned)((I + 255) / 256), 256, 0, st>>>(I, P.n_yt, P.ctas, kTcParts, P.part,
+                                                                        P.normX, scale, nullptr, P.off);
+  WOTG_LAUNCHED();
+  cudaEvent_t e0, e1;
+  WOTG_CUDA(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    set_last_error("cudaEventCreate", cudaGetLastError());
+    return WOTG_CUDA_ERROR;
+  }
+  cudaError_t e = cudaEventRecord(e0, st);
+  for (int k = 0; k < n_launch && e == cudaSuccess && s == WOTG_OK; ++k)
+    s = tc_lse_launch(P.Xa, P.n_xt, P.Yb, P.n_yt, P.kp, P.ctas, P.part, speculative ? P.off : nullptr, P.err, st);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s) return s;
+  if (e != cudaSuccess) {
+    set_last_error("lse_points timing", e);
+    return WOTG_CUDA_ERROR;
+  }
+  int err = 0;
+  WOTG_CUDA(cudaMemcpy(&err, P.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    set_last_message("tensor-core half-step: a bounded wait timed out");
+    return WOTG_CUDA_ERROR;
+  }
+  *ms_per_launch = ms / (float)n_launch;
   return WOTG_OK;
 }
