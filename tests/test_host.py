@@ -112,3 +112,23 @@ def test_no_cpu_fallback_without_gpu():
         pytest.skip('a GPU is present')
     with pytest.raises(RuntimeError, match='CUDA device'):
         wot_gb300.ot.optimal_transport_duality_gap(np.zeros((2, 2)), np.ones(2), 1, 50, 0.05, 5, 1e-8, 1e4, 1, 1e7)
+
+
+def test_centred_gram_identity():
+    """The PCA's Gram matrix from x^T x (dense and sparse products) equals the
+    Gram matrix of the explicitly double-centred matrix (wot/ot/util.py:240-255:
+    gene means removed, then each cell centred over genes), to FP64 rounding."""
+    import torch
+    from wot_gb300.ot.util import centred_gram
+    rng = np.random.default_rng(7)
+    x = rng.random((900, 150))
+    x[rng.random(x.shape) < 0.9] = 0.0
+    X = torch.tensor(np.log1p(5 * x))
+    mu = X.mean(dim=0)
+    xt = (X - mu).T
+    xt = xt - xt.mean(dim=0, keepdim=True)
+    ref = xt @ xt.T
+    for sparse in (False, True, None):
+        G = centred_gram(X, mu, sparse=sparse)
+        assert float((G - ref).abs().max() / ref.abs().max()) < 1e-13
+        assert torch.equal(G, G.T) or float((G - G.T).abs().max()) < 1e-15 * float(ref.abs().max())
