@@ -144,15 +144,20 @@ def coords_on_device(X, day):
     return (x0 * s).float().contiguous(), (x1 * s).float().contiguous()
 
 
-def cpu_sample(a, b, G, I_s, J_s, rng):
+def cpu_sample(a, b, G, I_s, J_s, rng, stages=None):
     """Oracle (FP64 NumPy restatement) on a random cell subsample; returns
-    (seconds, iterations, coupling, (a_s, b_s, G_s))."""
+    (seconds, iterations, coupling, (a_s, b_s, G_s)). With ``stages`` (a dict),
+    also the split of those seconds into cost and solve, and the subsampled
+    rows ('rows': (ri, rj))."""
     from oracle import ot_model as oom, optimal_transport as oot
     ri = np.sort(rng.choice(a.shape[0], I_s, replace=False))
     rj = np.sort(rng.choice(b.shape[0], J_s, replace=False))
     a_s, b_s, G_s = a[ri].astype(np.float64), b[rj].astype(np.float64), G[ri]
     t0 = time.perf_counter()
     C = oom.compute_default_cost_matrix(a_s, b_s)
+    if stages is not None:
+        stages['cost'] = time.perf_counter() - t0
+        stages['rows'] = (ri, rj)
     iters = [0]
 
     def counting(**kw):
@@ -161,7 +166,10 @@ def cpu_sample(a, b, G, I_s, J_s, rng):
         iters[0] += st['iterations']
         return out
 
+    t1 = time.perf_counter()
     T, _ = oot.compute_transport_matrix(solver=counting, C=C, G=G_s.copy(), **CFG)
+    if stages is not None:
+        stages['solve'] = time.perf_counter() - t1
     return time.perf_counter() - t0, iters[0], T, (a_s, b_s, G_s)
 
 
@@ -686,7 +694,14 @@ def main():
     if rank == 0 and not args.no_cpu:
         rng = np.random.default_rng(0)
         a_h, b_h, G_h = a.double().cpu().numpy(), b.double().cpu().numpy(), growth[day == 0]
-        t_cpu, it_cpu, T_cpu, (a_s, b_s, G_s) = cpu_sample(a_h, b_h, G_h, SAMPLE[0], SAMPLE[1], rng)
+        stages = {}
+        t_cpu, it_cpu, T_cpu, (a_s, b_s, G_s) = cpu_sample(a_h, b_h, G_h, SAMPLE[0], SAMPLE[1], rng, stages)
+        # the oracle's PCA of the same subsampled cells, timed apart from the solve
+        from oracle import ot_model as oom
+        ri, rj = stages.pop('rows')
+        tp = time.perf_counter()
+        oom.compute_pca(X[day == 0][ri], X[day == 1][rj], PCA_D)
+        stages['pca'] = time.perf_counter() - tp
         scale = (I_FULL * J_FULL) / (SAMPLE[0] * SAMPLE[1])
         it_gpu = iters / args.steps
         cpu_value = 1.0 / (t_cpu * scale * (it_gpu / it_cpu))
@@ -698,7 +713,8 @@ def main():
         line['cpu_baseline'] = {'value': cpu_value, 'unit': 'maps/s', 'cores': blas_threads(), 'kind': 'port',
                                 'sample': '%dx%d random subsample of the pair, full FP64 oracle solve with 3 growth '
                                           'iterations (%.1f s, %d iterations); extrapolated to 20000x25000 by '
-                                          'I*J*iterations' % (SAMPLE[0], SAMPLE[1], t_cpu, it_cpu)}
+                                          'I*J*iterations' % (SAMPLE[0], SAMPLE[1], t_cpu, it_cpu),
+                                'sample_stages_s': {k: round(v, 3) for k, v in stages.items()}}
 
     if extra:
         # the batched time course (one warm-up, one timed batch) and the large-pair chain
