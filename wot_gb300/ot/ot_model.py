@@ -13,6 +13,7 @@ from __future__ import annotations
 import itertools
 import logging
 import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -153,24 +154,37 @@ class OTModel:
             cost_matrices = [None for _ in day_pairs]
         learned_tables = []
         save_learned_growth = self.ot_config.get('growth_iters', 1) > 1
-        for day_pair, cost_matrix in zip(day_pairs, cost_matrices):
-            path = tmap_prefix
-            if not with_covariates:
-                path += "_{}_{}".format(*day_pair)
-            else:
-                path += "_{}_{}_cv{}_cv{}".format(*day_pair)
-            output_file = check_file_extension(os.path.join(tmap_dir, path), output_file_format)
-            if os.path.exists(output_file) and not overwrite:
-                logger.info('Found existing tmap at ' + output_file + '. ')
-                continue
-            if with_covariates:
-                tmap = self.compute_transport_map(day_pair[0], day_pair[1], covariate=day_pair[2],
-                                                  cost_matrix=cost_matrix)
-            else:
-                tmap = self.compute_transport_map(*day_pair, cost_matrix=cost_matrix)
-            write_dataset(tmap, output_file, output_format=output_file_format)
-            if save_learned_growth:
-                learned_tables.append(tmap.obs)
+        # each map is written by one background thread while the next one is
+        # computed; at most one write is in flight, and a failed write raises
+        # here before the next map is handed over (or at the end)
+        writer = ThreadPoolExecutor(max_workers=1)
+        pending = None
+        try:
+            for day_pair, cost_matrix in zip(day_pairs, cost_matrices):
+                path = tmap_prefix
+                if not with_covariates:
+                    path += "_{}_{}".format(*day_pair)
+                else:
+                    path += "_{}_{}_cv{}_cv{}".format(*day_pair)
+                output_file = check_file_extension(os.path.join(tmap_dir, path), output_file_format)
+                if os.path.exists(output_file) and not overwrite:
+                    logger.info('Found existing tmap at ' + output_file + '. ')
+                    continue
+                if with_covariates:
+                    tmap = self.compute_transport_map(day_pair[0], day_pair[1], covariate=day_pair[2],
+                                                      cost_matrix=cost_matrix)
+                else:
+                    tmap = self.compute_transport_map(*day_pair, cost_matrix=cost_matrix)
+                if pending is not None:
+                    pending.result()
+                pending = writer.submit(write_dataset, tmap, output_file, output_format=output_file_format)
+                if save_learned_growth:
+                    learned_tables.append(tmap.obs)
+                tmap = None
+            if pending is not None:
+                pending.result()
+        finally:
+            writer.shutdown(wait=True)
         if learned_tables:
             write_learned_growth(learned_tables, os.path.join(tmap_dir, tmap_prefix + '_g.txt'))
 
