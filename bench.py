@@ -47,9 +47,10 @@ def parse():
     ap.add_argument('--pair', default=None, help='I,J cells of a smaller pair (profiling runs)')
     ap.add_argument('--pca', type=int, default=None, help='local PCA dimension of the pair workload (profiling runs)')
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--workload', default='pair', choices=['pair', 'course', 'chain'],
+    ap.add_argument('--workload', default='pair', choices=['pair', 'course', 'chain', 'adjoint'],
                     help="pair: one 20000x25000 map per step; course: the batched 41-day time course x "
-                         "5x5 epsilon/lambda1 sweep (1000 maps) per step")
+                         "5x5 epsilon/lambda1 sweep (1000 maps) per step; chain: the 60000x60000 map and "
+                         "the 20-map chain; adjoint: objective + gradient of a 10000x12000 pair")
     ap.add_argument('--course-days', type=int, default=41)
     ap.add_argument('--no-extra', action='store_true',
                     help='pair workload only: skip the batched-course and chain summaries of the JSON line')
@@ -376,6 +377,51 @@ def chain_days(big=60000, n_chain=21, lo=20000, hi=60000, seed=4):
     return sizes, days
 
 
+def run_adjoint(args, data=None):
+    """The gradient workload: the converged unbalanced OT objective of a
+    10000 x 12000 pair of 30-d points (10-component mixture, log g ~ N(0, 0.3^2),
+    eps 0.05, lambda1 1, lambda2 50) and its gradient with respect to both point
+    sets and log g, through wot_gb300.ot.adjoint.ot_objective (duality-gap solve,
+    400 refinement iterations at the final epsilon, one adjoint pass per side)."""
+    import torch
+    from wot_gb300 import _native, synthetic
+    from wot_gb300.ot import device as D
+    from wot_gb300.ot.adjoint import ot_objective
+    lib = _native.load()
+    I, J, d = 10000, 12000, 30
+    x = torch.tensor(synthetic.gaussian_mixture_points(I, d=d, n_components=10, seed=31), device='cuda')
+    y = torch.tensor(synthetic.gaussian_mixture_points(J, d=d, n_components=10, seed=32), device='cuda')
+    lg = torch.tensor(np.random.default_rng(33).normal(0.0, 0.3, I), device='cuda')
+    c = D.cost_from_points(x.float(), y.float())
+    scale = 1.0 / D.median(c)
+    del c
+
+    def step():
+        xt, yt, lt = (t.clone().requires_grad_(True) for t in (x, y, lg))
+        obj = ot_objective(xt, yt, lt, epsilon=0.05, lambda1=1.0, lambda2=50.0, cost_scale=scale)
+        obj.backward()
+        return obj, xt.grad
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    n_launch0 = lib.wotg_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        obj, gx = step()
+    ev1.record()
+    torch.cuda.synchronize()
+    t = ev0.elapsed_time(ev1) / 1e3
+    return {'value': args.steps / t, 'unit': 'objective+gradient/s', 'ms_per_step': t / args.steps * 1e3,
+            'steps': args.steps, 'warmup': args.warmup, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': 'unbalanced OT objective and its gradient w.r.t. x, y, log g: 10000 x 12000 '
+                                   '30-d mixture points, eps 0.05, lambda1 1, lambda2 50, duality-gap solve + '
+                                   '400 refinement iterations + adjoint', 'I': I, 'J': J, 'd': d},
+            'objective': float(obj), 'grad_x_abs_sum': float(gx.abs().sum()),
+            'gpu_launches': int(lib.wotg_launch_count() - n_launch0)}
+
+
 def run_chain(args, data):
     """The large-pair workload: one 60000 x 60000 map in 50-d local PCA on the
     on-the-fly form, then 20 maps of 20000-60000 cells held as potentials and a
@@ -511,6 +557,11 @@ def main():
         import torch
         torch.cuda.set_device(dist_env()[2])
         print(json.dumps(run_chain(args, data)), flush=True)
+        return
+    if args.workload == 'adjoint' and args.impl != 'reference':
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        print(json.dumps(run_adjoint(args)), flush=True)
         return
     if args.workload == 'course' and args.impl != 'reference':
         data = course_days(args.course_days)
@@ -717,10 +768,11 @@ def main():
                                 'sample_stages_s': {k: round(v, 3) for k, v in stages.items()}}
 
     if extra:
-        # the batched time course (one warm-up, one timed batch) and the large-pair chain
+        # the batched time course (one warm-up, one timed batch), the large-pair chain and the gradient
         sub = argparse.Namespace(**vars(args))
         sub.steps, sub.warmup, sub.quick = 1, 1, True
-        for key, fn, data in (('course', run_course, course_data), ('chain', run_chain, chain_data)):
+        for key, fn, data in (('course', run_course, course_data), ('chain', run_chain, chain_data),
+                              ('adjoint', run_adjoint, None)):
             try:
                 if isinstance(data, tuple) and len(data) == 2 and isinstance(data[0], str):
                     raise RuntimeError(data[1])

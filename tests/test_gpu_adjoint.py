@@ -84,3 +84,35 @@ def test_adjoint_vs_finite_differences(problem):
         scale = max(abs(f) for _, f in sel)
         err = max(abs(a - f) for a, f in sel)
         assert err <= GRAD_TOL * max(scale, float(g[name].abs().max())), (name, err, scale)
+
+
+def test_adjoint_directional_derivative_full_size():
+    """At the full 10000 x 12000 size (30-d points from a 10-component mixture,
+    log g ~ N(0, 0.3^2)), where no FP64 oracle runs: the gradient's directional
+    derivative along its own sign pattern, <g, sign(g)> = |g|_1, against the
+    central difference of the converged objective (each a full solve + refine)
+    with every coordinate moved by 1e-3. Tolerance 1e-3 relative."""
+    import torch
+    from wot_gb300 import synthetic
+    from wot_gb300.ot.adjoint import ot_objective
+    I, J, d, h = 10000, 12000, 30, 1e-3
+    x = torch.tensor(synthetic.gaussian_mixture_points(I, d=d, n_components=10, seed=31), device='cuda')
+    y = torch.tensor(synthetic.gaussian_mixture_points(J, d=d, n_components=10, seed=32), device='cuda')
+    lg = torch.tensor(np.random.default_rng(33).normal(0.0, 0.3, I), device='cuda')
+    from wot_gb300.ot import device as D
+    # the cost scale (1/median of the unperturbed cost) stays fixed across the three objectives
+    c = D.cost_from_points(x.float(), y.float())
+    scale = 1.0 / D.median(c)
+    del c
+    xt, yt, lt = (t.clone().requires_grad_(True) for t in (x, y, lg))
+    obj = ot_objective(xt, yt, lt, epsilon=EPS, lambda1=L1, lambda2=L2, cost_scale=scale)
+    obj.backward()
+    sx, sy, sl = torch.sign(xt.grad), torch.sign(yt.grad), torch.sign(lt.grad)
+    ana = float(xt.grad.abs().sum() + yt.grad.abs().sum() + lt.grad.abs().sum())
+    with torch.no_grad():
+        dp = float(ot_objective(x + h * sx, y + h * sy, lg + h * sl, epsilon=EPS, lambda1=L1, lambda2=L2,
+                                cost_scale=scale))
+        dm = float(ot_objective(x - h * sx, y - h * sy, lg - h * sl, epsilon=EPS, lambda1=L1, lambda2=L2,
+                                cost_scale=scale))
+    fd = (dp - dm) / (2 * h)
+    assert abs(fd - ana) <= 1e-3 * abs(ana), (fd, ana)
