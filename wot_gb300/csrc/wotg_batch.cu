@@ -486,8 +486,8 @@ __device__ __forceinline__ void run_single(const PassArgs& A, const Seg& sg, int
   if (lane == 0) s_vmax[warp][0] = vmax;
 }
 
-template <int KG, int RW, bool SPEC, int MINB = 1>
-__global__ void __launch_bounds__(kThreads, MINB) pass_kernel(PassArgs A) {
+template <int KG, int RW, bool SPEC>
+__global__ void __launch_bounds__(kThreads) pass_kernel(PassArgs A) {
   __shared__ __align__(16) float sW[2][KG][kChunk];
   __shared__ Entry gp[KG];
   __shared__ double s_vmax[kWarps][KG];
@@ -1039,15 +1039,11 @@ struct PassCfg {
   PassFn spec, exact;
 };
 
-// The last two are register-capped copies (<= 80 and <= 64 registers: 3 and 4
-// resident CTAs of 256 threads instead of 2 and 3) for latency hiding.
 static const PassCfg kCfgs[] = {
     {8, 1, pass_kernel<8, 1, true>, pass_kernel<8, 1, false>},
     {8, 2, pass_kernel<8, 2, true>, pass_kernel<8, 2, false>},
     {16, 1, pass_kernel<16, 1, true>, pass_kernel<16, 1, false>},
     {16, 2, pass_kernel<16, 2, true>, pass_kernel<16, 2, false>},
-    {16, 1, pass_kernel<16, 1, true, 3>, pass_kernel<16, 1, false, 3>},
-    {8, 1, pass_kernel<8, 1, true, 4>, pass_kernel<8, 1, false, 4>},
 };
 constexpr int kNumCfgs = sizeof(kCfgs) / sizeof(kCfgs[0]);
 
