@@ -132,3 +132,46 @@ def test_centred_gram_identity():
         G = centred_gram(X, mu, sparse=sparse)
         assert float((G - ref).abs().max() / ref.abs().max()) < 1e-13
         assert torch.equal(G, G.T) or float((G - G.T).abs().max()) < 1e-15 * float(ref.abs().max())
+
+
+def test_invalid_arguments_rejected_before_device_work():
+    """Every compute entry point of the C ABI checks its arguments before it
+    touches the device: NULL pointers, empty or misaligned shapes and
+    non-positive parameters return WOTG_BADARG (the reference's ValueError,
+    through _native.check) on a machine without a GPU. No kernel runs here."""
+    from wot_gb300 import _build
+    _build.build()
+    lib = _native.load()
+    BAD = _native.WOTG_BADARG
+    f = ctypes.c_float
+    d = ctypes.c_double(0.0)
+    assert lib.wotg_median(None, 10, 10, 12, ctypes.byref(d), None, 0, None) == BAD
+    assert lib.wotg_median(None, 10, 10, 10, ctypes.byref(d), None, 0, None) == BAD   # ldc not a multiple of 4
+    assert lib.wotg_compute_transport_matrix(None, None, None, None, None, None, None, None, None, 0, None) == BAD
+    assert lib.wotg_compute_transport_matrix_noalloc(None, None, None, None, None, None, None, None, None) == BAD
+    assert lib.wotg_refine_potentials(None, None, 0.05, 10, None, None, None, None, 0, None) == BAD
+    assert lib.wotg_lse_matvec(None, 4, 4, 4, None, f(1.0), 0, None, None, 0, None) == BAD
+    assert lib.wotg_lse_points(None, 4, 4, None, 4, 4, 4, 1.0, None, None, None, 0, None) == BAD
+    r = ctypes.c_float(0.0)
+    assert lib.wotg_lse_points_timing(None, 4, 4, None, 4, 4, 4, 1.0, None, 1, 0, ctypes.byref(r), None, 0,
+                                      None) == BAD
+    assert lib.wotg_apply_coupling_f64(None, 3, 3, None, 0, 0, 0, None, None) == BAD
+    assert lib.wotg_transpose_cost(None, 3, 3, 4, None, 3, None) == BAD
+    assert lib.wotg_solve_batched(None, 0, None, 0, None, None, None, None, None, None, None, 0, None) == BAD
+    k2 = (ctypes.c_float * 1)(1.0)
+    assert lib.wotg_lse_matvec_multi(None, 4, 4, 4, None, 4, k2, 1, None, 4, None, 0, None) == BAD
+    assert lib.wotg_coupling_from_potentials(None, 3, 3, 4, 1.0, 0.0, None, None, 0.0, None, None) == BAD
+    assert lib.wotg_ot_adjoint(None, 3, 2, None, 3, 2, 2, 1.0, 0.05, 1.0, 50.0, None, None, None, None, None, None,
+                               ctypes.byref(d), None, 0, None) == BAD
+    assert lib.wotg_exp2_rate(None, None) == BAD
+    # workspace queries of impossible shapes are 0
+    assert lib.wotg_lse_points_workspace_bytes(0, 5, 4) == 0
+    assert lib.wotg_lse_points_workspace_bytes(5, 5, 200) == 0
+    # the status -> exception mapping of the reference
+    with pytest.raises(ValueError):
+        _native.check(BAD, 'x')
+    with pytest.raises(ValueError):
+        _native.check(_native.WOTG_WORKSPACE, 'x')
+    with pytest.raises(RuntimeError, match='Overflow encountered in duality gap'):
+        _native.check(_native.WOTG_NONFINITE, 'x')
+    assert _native.check(_native.WOTG_MAX_ITER, 'x') == _native.WOTG_MAX_ITER
