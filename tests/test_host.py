@@ -175,3 +175,26 @@ def test_invalid_arguments_rejected_before_device_work():
     with pytest.raises(RuntimeError, match='Overflow encountered in duality gap'):
         _native.check(_native.WOTG_NONFINITE, 'x')
     assert _native.check(_native.WOTG_MAX_ITER, 'x') == _native.WOTG_MAX_ITER
+
+
+def test_synthetic_inputs_have_the_stated_distributions():
+    """The seeded inputs every measurement uses: about 90 % zero counts,
+    log1p(CP10k) values, lognormal(0, 0.3) growth, pure functions of the seed;
+    course days are independent of the order they are generated in."""
+    from wot_gb300 import synthetic
+    X, day, g = synthetic.time_course([600, 700], n_genes=300, n_clusters=6, seed=3)
+    assert X.shape == (1300, 300) and sorted(set(day.tolist())) == [0.0, 1.0]
+    assert 0.85 <= float((X == 0).mean()) <= 0.95
+    assert np.allclose(np.expm1(X).sum(axis=1)[np.expm1(X).sum(axis=1) > 0], 1e4, rtol=1e-9)
+    lg = np.log(g)
+    assert abs(lg.mean()) < 0.05 and abs(lg.std() - 0.3) < 0.03
+    X2, day2, g2 = synthetic.time_course([600, 700], n_genes=300, n_clusters=6, seed=3)
+    assert np.array_equal(X, X2) and np.array_equal(g, g2)
+    prof = synthetic.course_profiles(5, n_genes=200, n_clusters=8, seed=1)
+    a = [synthetic.course_day(prof, t, 300) for t in range(5)]
+    b = [synthetic.course_day(prof, t, 300) for t in reversed(range(5))][::-1]
+    for (xa, ga), (xb, gb) in zip(a, b):
+        assert np.array_equal(xa, xb) and np.array_equal(ga, gb)
+    assert 0.8 <= float(np.mean([(x == 0).mean() for x, _ in a])) <= 0.95
+    sizes = synthetic.log_uniform_day_sizes(41)
+    assert sizes.min() >= 1000 and sizes.max() <= 30000
