@@ -99,7 +99,7 @@ def unrolled_gradient(x, y, logg, eps, lambda1, lambda2, scale, ubar0, vbar0, n_
                          n_unroll)
     D = dual(C, p, q, ubar, vbar, eps, lambda1, lambda2)
     D.backward()
-    return float(D), x.grad, y.grad, logg.grad
+    return float(D.detach()), x.grad, y.grad, logg.grad
 
 
 def fd_gradient(x, y, logg, eps, lambda1, lambda2, scale, coords, ubar0, vbar0, h=1e-4, dt=1.0, tol=1e-13):
