@@ -714,7 +714,10 @@ def main():
             'warmup': args.warmup, 'ms_per_step': t / args.steps * 1e3, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
             'config': {'workload': WORKLOAD, 'I': I_FULL, 'J': J_FULL, 'd': PCA_D, 'parallelism': 'replicas' if world > 1 else 'single',
-                       'l2': 'inputs larger than L2 (FP32 cost 2.0 GB per pass)',
+                       'l2': ('inputs larger than L2: every step writes the 2.0 GB FP32 cost and the 4.0 GB '
+                              'FP64 map, so nothing of one step stays in L2 for the next; the materialised '
+                              'form streams the cost every half-step, the on-the-fly form re-reads its 5.8 MB '
+                              'of packed points from L2 within a step'),
                        'timed': 'cost + median + 3 duality-gap solves + dense FP64 coupling, coordinates resident'},
             'sinkhorn_iter_per_s': iters / t * world, 'iterations_per_map': iters / args.steps,
             'roofline': roofline, 'roofline_materialized': roof_mat, 'roofline_onthefly': roof_tc,
