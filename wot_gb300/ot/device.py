@@ -135,14 +135,15 @@ def make_params(cfg: dict, solver: int) -> N.Params:
 
 
 FORMS = {'materialized': N.FORM_MATERIALIZED, 'onthefly': N.FORM_ONTHEFLY}
+TC_MAX_DIM = 62   # point dimensions the tensor-core half-step packs (two bias columns in 64)
 
 
 def resolve_form(cost: DeviceCost, form: str) -> int:
     """'materialized' streams the FP32 cost; 'onthefly' recomputes cost tiles
     from the points on the tensor cores; 'auto' picks the latter when the cost
-    was built from points of at most 64 dimensions."""
+    was built from points of at most TC_MAX_DIM dimensions."""
     if form == 'auto':
-        form = 'onthefly' if cost.X is not None and cost.X.shape[1] <= 64 else 'materialized'
+        form = 'onthefly' if cost.X is not None and cost.X.shape[1] <= TC_MAX_DIM else 'materialized'
     if form not in FORMS:
         raise ValueError("form must be 'auto', 'materialized' or 'onthefly'")
     if form == 'onthefly' and cost.X is None:
