@@ -198,3 +198,20 @@ def test_synthetic_inputs_have_the_stated_distributions():
     assert 0.8 <= float(np.mean([(x == 0).mean() for x, _ in a])) <= 0.95
     sizes = synthetic.log_uniform_day_sizes(41)
     assert sizes.min() >= 1000 and sizes.max() <= 30000
+
+
+def test_batch_item_statuses_follow_the_reference(caplog):
+    """Per-item outcomes of a batched solve: max_iter items log the reference's
+    warning (optimal_transport.py:143-145), a NaN duality gap raises its
+    RuntimeError (:162-163) unless asked to keep the batch."""
+    import logging
+    from wot_gb300.ot.batch import report_statuses
+    OK, MAXIT, NAN = _native.WOTG_OK, _native.WOTG_MAX_ITER, _native.WOTG_NONFINITE
+    with caplog.at_level(logging.WARNING, logger='wot'):
+        assert report_statuses([OK, MAXIT, OK]) == []
+    assert any('Reached max_iter' in r.getMessage() for r in caplog.records)
+    with pytest.raises(RuntimeError, match='Overflow encountered in duality gap.*items 1, 3'):
+        report_statuses([OK, NAN, OK, NAN])
+    assert report_statuses([NAN, OK], raise_nonfinite=False) == [0]
+    with pytest.raises(RuntimeError, match='status 4'):
+        report_statuses([_native.WOTG_CUDA_ERROR])

@@ -56,9 +56,32 @@ class ImplicitMap(ImplicitCoupling):
         self.status = status
 
 
-def solve_batched(pairs, items):
+def report_statuses(statuses, raise_nonfinite=True):
+    """The reference's per-map outcomes for a batch's item statuses: the
+    max_iter warning (optimal_transport.py:143-145) for each item that hit
+    max_iter, and the RuntimeError of a NaN duality gap (optimal_transport.py:
+    162-163) when any item ended non-finite (unless raise_nonfinite is False)."""
+    bad = []
+    for k, s in enumerate(statuses):
+        s = int(s)
+        if s == N.WOTG_MAX_ITER:
+            N.check(s, 'wotg_solve_batched item %d' % k)
+        elif s == N.WOTG_NONFINITE:
+            bad.append(k)
+        elif s != N.WOTG_OK:
+            raise RuntimeError('wotg_solve_batched item %d: status %d' % (k, s))
+    if bad and raise_nonfinite:
+        raise RuntimeError('Overflow encountered in duality gap computation, please report this incident '
+                           '(batch items %s)' % ', '.join(str(k) for k in bad))
+    return bad
+
+
+def solve_batched(pairs, items, raise_nonfinite=True):
     """Solve every item; ``items`` is a list of (pair index, config dict) with the
-    reference's ot_config keys (duality-gap solver). Returns one ImplicitMap per item."""
+    reference's ot_config keys (duality-gap solver). Returns one ImplicitMap per item
+    (its ``status`` the item's wotg status). Items that hit max_iter log the
+    reference's warning; an item whose duality gap became NaN raises the
+    reference's RuntimeError unless raise_nonfinite is False."""
     torch = N.require_cuda()
     lib = N.load()
     np_, ni = len(pairs), len(items)
@@ -95,6 +118,7 @@ def solve_batched(pairs, items):
     N.check(lib.wotg_solve_batched(hp, np_, hi, ni, u_bar.data_ptr(), v_bar.data_ptr(), row_sums.data_ptr(),
                                    learned.data_ptr(), stats, statuses, ws.data_ptr(), nbytes, D._stream()),
             'wotg_solve_batched')
+    report_statuses(statuses, raise_nonfinite)
     out = []
     for k, (p, cfg) in enumerate(items):
         ro, co, go, gi = offs[k]
