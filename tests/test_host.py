@@ -215,3 +215,47 @@ def test_batch_item_statuses_follow_the_reference(caplog):
     assert report_statuses([NAN, OK], raise_nonfinite=False) == [0]
     with pytest.raises(RuntimeError, match='status 4'):
         report_statuses([_native.WOTG_CUDA_ERROR])
+
+
+def test_otmodel_configuration_without_a_gpu(tmp_path, caplog):
+    """OTModel's constructor and pair bookkeeping (wot/ot/ot_model.py:37-114,
+    203-216) need no device: defaults and their precedence (kwargs, then the
+    parameter file), solver choice, local_pca above the gene count, NaN days,
+    day and cell filters, per-day subsampling, timepoints, the day_pairs check."""
+    import logging
+    import wot_gb300 as wot
+    rng = np.random.default_rng(0)
+    ids = np.array(['c%d' % i for i in range(12)])
+    day = np.array([0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, np.nan])
+    ds = Dataset(rng.random((12, 5)), Frame({'day': day}, index=ids), Frame(index=np.array(list('abcde'))))
+    pf = tmp_path / 'params.txt'
+    pf.write_text('epsilon\t0.02\n')
+    with caplog.at_level(logging.WARNING, logger='wot'):
+        m = wot.OTModel(ds, epsilon=0.1, lambda1=3, parameters=str(pf))
+    assert any('Disabling PCA' in r.getMessage() for r in caplog.records)
+    assert m.ot_config['local_pca'] == 0 and m.ot_config['epsilon'] == 0.02 and m.ot_config['lambda1'] == 3
+    assert m.ot_config['lambda2'] == 50 and m.ot_config['tolerance'] == 1e-8 and m.ot_config['batch_size'] == 5
+    assert m.timepoints == [0.0, 1.0, 2.0] and m.matrix.shape[0] == 11          # the NaN day is dropped
+    assert m.solver is wot.ot.optimal_transport_duality_gap
+    assert wot.OTModel(ds, solver='fixed_iters').solver is wot.ot.transport_stablev2
+    with pytest.raises(ValueError, match='Unknown solver'):
+        wot.OTModel(ds, solver='other')
+    with pytest.raises(ValueError, match='Days information'):
+        wot.OTModel(ds, day_field='time')
+    assert wot.OTModel(ds, cell_day_filter='0,2').timepoints == [0.0, 2.0]
+    kept = wot.OTModel(ds, cell_filter=['c1', 'c2', 'c5'])
+    assert list(kept.matrix.obs.index) == ['c1', 'c2', 'c5']
+    assert wot.OTModel(ds, gene_filter=['b', 'd']).matrix.X.shape[1] == 2
+    sub = wot.OTModel(ds, ncells=2)
+    assert sorted(np.unique(sub.matrix.obs['day'], return_counts=True)[1].tolist()) == [2, 2, 2]
+    with pytest.raises(ValueError, match='No cells'):
+        wot.OTModel(ds, cell_filter=['nobody'])
+    cf = tmp_path / 'pairs.txt'
+    cf.write_text('t0\tt1\tepsilon\n0\t1\t0.1\n')
+    pairs = wot.OTModel(ds, config=str(cf))
+    with pytest.raises(ValueError, match='not present in day_pairs'):
+        pairs.compute_transport_map(1, 2)
+    # contiguous day rows are selected as views of X
+    p0, p1 = m.select_pair({'t0': 0, 't1': 1, 'covariate': None})
+    assert p0.X.base is not None and np.shares_memory(p0.X, m.matrix.X)
+    assert p0.shape == (4, 5) and p1.shape == (4, 5)
