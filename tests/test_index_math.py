@@ -27,3 +27,9 @@ def test_tensor_core_partition(tmp_path):
     """lse_tc_kernel's stretches and the combine's partial lookup
     (tc_stretch_begin / tc_cta_of): unique in-bounds slots, complete reads."""
     _run('stretch_check', tmp_path)
+
+
+def test_tensor_core_operand_layout(tmp_path):
+    """Packed tile offsets and the MMA's shared-memory descriptors agree
+    (core_offset / smem_desc / idesc_f16_f32 in wotg_tc.cuh)."""
+    _run('layout_check', tmp_path)
