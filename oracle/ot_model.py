@@ -7,6 +7,12 @@
   coordinates agree with the reference up to sign/rotation within the top
   subspace and to randomized-SVD error; parity of the solver is therefore
   pinned on shared coordinates (both sides fed the same ``p0_x``, ``p1_x``).
+* ``compute_pca_reference``       — the same PCA as the reference computes it:
+  scikit-learn's solver choice and, for its randomized solver, the randomized
+  range finder (Halko, Martinsson, Tropp 2011, Alg. 4.4) with LU-normalised
+  power iterations, seeded by ``numpy.random.RandomState(58951)``, restated
+  with NumPy / SciPy calls; pinned to the reference's own output in
+  ``tests/golden/pair_120x150.npz`` and to scikit-learn where it is installed.
 * ``compute_default_cost_matrix`` — wot/ot/ot_model.py:242-253 (coordinates
   scaled by the singular values, squared Euclidean as
   ``|x|^2 - 2 x.y + |y|^2`` clipped at 0 like scikit-learn's
@@ -55,6 +61,48 @@ def sqeuclidean(a, b):
     return d
 
 
+def compute_pca_reference(m1, m2, n_components, seed=58951, n_oversamples=10):
+    """The reference's PCA (wot/ot/util.py:240-255: scikit-learn
+    ``PCA(n_components, random_state=58951).fit(x.T)``) restated: returns
+    ``(pca_1, pca_2, singular_values, mean_shift, solver)``."""
+    import scipy.linalg as sl
+    x = np.vstack([np.asarray(m1, dtype=np.float64), np.asarray(m2, dtype=np.float64)])
+    mean_shift = x.mean(axis=0)
+    x = x - mean_shift
+    k = min(n_components, x.shape[0])
+    data = x.T                                   # genes x cells: genes are the samples
+    data = data - data.mean(axis=0)              # PCA centring of each feature (cell)
+    n_s, n_f = data.shape
+    if n_f <= 1000 and n_s >= 10 * n_f:
+        solver = 'covariance_eigh'
+    elif max(n_s, n_f) <= 500:
+        solver = 'full'
+    elif 1 <= k < 0.8 * min(n_s, n_f):
+        solver = 'randomized'
+    else:
+        solver = 'full'
+    if solver == 'randomized':
+        n_iter = 7 if k < 0.1 * min(n_s, n_f) else 4
+        transpose = n_s < n_f
+        M = data.T if transpose else data
+        Q = np.random.RandomState(seed).normal(size=(M.shape[1], k + n_oversamples))
+        for _ in range(n_iter):
+            Q, _ = sl.lu(M @ Q, permute_l=True)
+            Q, _ = sl.lu(M.T @ Q, permute_l=True)
+        Q, _ = sl.qr(M @ Q, mode='economic')
+        Uh, s, Vt = sl.svd(Q.T @ M, full_matrices=False)
+        comp = (Q @ Uh)[:, :k].T if transpose else Vt[:k]       # k x cells
+        s = s[:k]
+    else:
+        _, s, vt = np.linalg.svd(data, full_matrices=False)
+        comp, s = vt[:k], s[:k]
+    i = np.argmax(np.abs(comp), axis=1)
+    comp = comp * np.sign(comp[np.arange(comp.shape[0]), i])[:, None]
+    comp = comp.T
+    n1 = np.asarray(m1).shape[0]
+    return comp[:n1], comp[n1:], s, mean_shift, solver
+
+
 def compute_default_cost_matrix(a, b, eigenvals=None):
     """Median-normalised squared-Euclidean cost (wot/ot/ot_model.py:242-253)."""
     if eigenvals is not None:
@@ -64,12 +112,13 @@ def compute_default_cost_matrix(a, b, eigenvals=None):
     return c / np.median(c)
 
 
-def compute_single_transport_map(X, day, t0, t1, growth=None, C=None, solver='duality_gap',
+def compute_single_transport_map(X, day, t0, t1, growth=None, C=None, solver='duality_gap', pca='exact',
                                  **params):
     """One transport map from day ``t0`` to ``t1`` (wot/ot/ot_model.py:255-326).
 
     Returns ``(tmap, obs_growth)`` with ``obs_growth = {'g0': ..., ...}``, or
-    ``None`` when a day has no cells.
+    ``None`` when a day has no cells. ``pca`` 'exact' uses ``compute_pca``,
+    'reference' the reference's own PCA (``compute_pca_reference``).
     """
     config = dict(DEFAULT_CONFIG)
     config.update(params)
@@ -80,7 +129,10 @@ def compute_single_transport_map(X, day, t0, t1, growth=None, C=None, solver='du
     local_pca = config.pop('local_pca', None)
     eigenvals = None
     if local_pca is not None and local_pca > 0:
-        x0, x1, s, _ = compute_pca(X[sel0], X[sel1], local_pca)
+        if pca == 'reference':
+            x0, x1, s, _, _ = compute_pca_reference(X[sel0], X[sel1], local_pca)
+        else:
+            x0, x1, s, _ = compute_pca(X[sel0], X[sel1], local_pca)
         eigenvals = np.diag(s)
     else:
         x0, x1 = X[sel0], X[sel1]

@@ -240,6 +240,10 @@ def test_otmodel_configuration_without_a_gpu(tmp_path, caplog):
     assert wot.OTModel(ds, solver='fixed_iters').solver is wot.ot.transport_stablev2
     with pytest.raises(ValueError, match='Unknown solver'):
         wot.OTModel(ds, solver='other')
+    assert wot.OTModel(ds).pca == 'exact' and wot.OTModel(ds, pca='reference').pca == 'reference'
+    assert 'pca' not in wot.OTModel(ds, pca='reference').ot_config
+    with pytest.raises(ValueError, match='pca'):
+        wot.OTModel(ds, pca='randomized')
     with pytest.raises(ValueError, match='Days information'):
         wot.OTModel(ds, day_field='time')
     assert wot.OTModel(ds, cell_day_filter='0,2').timepoints == [0.0, 2.0]

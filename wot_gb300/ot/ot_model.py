@@ -41,7 +41,11 @@ class OTModel:
         ``ncounts``, ``ncells``, ``solver`` ('duality_gap' | 'fixed_iters'),
         ``parameters`` (2-column file), and any ot_config key. The GPU-only
         ``form`` ('auto' | 'materialized' | 'onthefly') picks how the cost is
-        read by the Sinkhorn half-steps; it is not part of ot_config.
+        read by the Sinkhorn half-steps, and ``pca`` ('exact' | 'reference') how
+        the local PCA is computed: the exact decomposition of the double-centred
+        matrix, or the reference's own scikit-learn PCA (randomized solver,
+        random_state 58951) reproduced to FP64 rounding; neither is part of
+        ot_config.
     """
 
     def __init__(self, matrix, day_field='day', covariate_field='covariate',
@@ -56,8 +60,12 @@ class OTModel:
         day_filter = kwargs.pop('cell_day_filter', None)
         ncounts = kwargs.pop('ncounts', None)
         ncells = kwargs.pop('ncells', None)
-        # GPU-only knob, kept out of ot_config: 'auto' | 'materialized' | 'onthefly'
+        # GPU-only knobs, kept out of ot_config: 'auto' | 'materialized' | 'onthefly', and
+        # the local PCA: 'exact' decomposition, or 'reference' (scikit-learn's solver and seed)
         self.form = kwargs.pop('form', 'auto')
+        self.pca = kwargs.pop('pca', 'exact')
+        if self.pca not in ('exact', 'reference'):
+            raise ValueError("pca must be 'exact' or 'reference'")
         self.matrix = _filter(self.matrix, cell_filter, gene_filter)
         if day_filter is not None:
             days = [float(day) for day in day_filter.split(',')] if isinstance(day_filter, str) else day_filter
@@ -215,7 +223,7 @@ class OTModel:
                 continue
             local_pca = config.get('local_pca')
             if local_pca is not None and local_pca > 0:
-                x0, x1, sv, _ = compute_pca(p0.X, p1.X, local_pca)
+                x0, x1, sv, _ = compute_pca(p0.X, p1.X, local_pca, solver=self.pca)
                 cost = OTModel.compute_default_cost_matrix(x0, x1, sv)
             else:
                 cost = OTModel.compute_default_cost_matrix(p0.X, p1.X)
@@ -297,7 +305,7 @@ class OTModel:
         local_pca = config.pop('local_pca', None)
         if config['C'] is None:
             if local_pca is not None and local_pca > 0:
-                x0, x1, s, _ = compute_pca(p0.X, p1.X, local_pca)
+                x0, x1, s, _ = compute_pca(p0.X, p1.X, local_pca, solver=self.pca)
                 config['C'] = OTModel.compute_default_cost_matrix(x0, x1, s)
             else:
                 config['C'] = OTModel.compute_default_cost_matrix(p0.X, p1.X)

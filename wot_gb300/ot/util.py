@@ -19,6 +19,19 @@ so only x^T x touches the cells. Expression matrices are mostly zeros
 (log1p of counts); below ``SPARSE_DENSITY`` nonzeros x^T x is a sparse-dense
 product (cuSPARSE, FP64) over the nonzeros instead of a dense FP64 GEMM, about
 1/density times fewer FMAs on a part whose FP64 rate is low.
+
+``solver='reference'`` instead reproduces the reference's decomposition itself:
+scikit-learn's choice of solver for this shape and, where that is its
+randomized solver, the randomized range finder of Halko, Martinsson and Tropp
+(SIAM Review 53(2), 2011, Algorithm 4.4 with a re-orthonormalised power
+iteration) with the reference's seed: the same Gaussian test matrix
+(``numpy.random.RandomState(58951)``), 10 oversampling columns, 7 (or 4) power
+iterations, then the SVD of the small projected matrix and the sign convention
+of the largest entry of each component. The products with the double-centred
+matrix run on the device from the sparse expression and rank-one centring
+terms; only 40 x 40 and 40 x genes factorisations run on the host. The result
+equals scikit-learn's to FP64 rounding (the subspace does not depend on how
+the iterates are re-orthonormalised).
 """
 from __future__ import annotations
 
@@ -55,14 +68,134 @@ def centred_gram(x, mu, sparse=None):
     return A - r[:, None] - r[None, :] + r.mean()
 
 
-def compute_pca(m1, m2, n_components):
+def sklearn_pca_solver(n_samples, n_features, n_components):
+    """scikit-learn's PCA(svd_solver='auto') choice (releases 1.5 and later) for
+    an n_samples x n_features data matrix; the reference fits genes x cells."""
+    if n_features <= 1000 and n_samples >= 10 * n_features:
+        return 'covariance_eigh'
+    if max(n_samples, n_features) <= 500:
+        return 'full'
+    if 1 <= n_components < 0.8 * min(n_samples, n_features):
+        return 'randomized'
+    return 'full'
+
+
+class _Centred:
+    """The reference's double-centred matrix as an operator, never formed:
+    T = x - 1 mu^T - c 1^T (cells x genes; mu the gene means, c each cell's mean
+    over genes after removing mu), i.e. the transpose of the matrix the
+    reference hands to scikit-learn. Products with T and T^T come from x (or
+    its sparse form) and two rank-one terms."""
+
+    def __init__(self, x, mu, sparse=None):
+        import torch
+        self.x, self.mu = x, mu
+        n, p = x.shape
+        self.c = (x @ torch.ones(p, dtype=x.dtype, device=x.device)) / p - float(mu.sum()) / p
+        if sparse is None:
+            sparse = int(torch.count_nonzero(x)) < SPARSE_DENSITY * x.numel()
+        self.xs = self.xts = None
+        if sparse:
+            with warnings.catch_warnings():         # torch marks sparse CSR as beta
+                warnings.simplefilter('ignore', UserWarning)
+                self.xs = x.to_sparse_csr()
+                self.xts = x.T.contiguous().to_sparse_csr()
+
+    def _mm(self, a, b):
+        import torch
+        if a is None:
+            return None
+        with warnings.catch_warnings():
+            warnings.simplefilter('ignore', UserWarning)
+            return torch.sparse.mm(a, b)
+
+    def t_mul(self, Q):
+        """T @ Q, Q genes x r."""
+        xq = self._mm(self.xs, Q) if self.xs is not None else self.x @ Q
+        return xq - (self.mu @ Q)[None, :] - self.c[:, None] * Q.sum(dim=0)[None, :]
+
+    def tt_mul(self, Q):
+        """T^T @ Q, Q cells x r."""
+        xq = self._mm(self.xts, Q) if self.xts is not None else self.x.T @ Q
+        return xq - self.mu[:, None] * Q.sum(dim=0)[None, :] - (self.c @ Q)[None, :]
+
+
+def _orthonormal(A):
+    """An orthonormal basis of A's columns: Cholesky QR twice, the r x r
+    factorisations on the host; Householder QR on the host when A's Gram
+    matrix is not positive definite (rank-deficient iterates)."""
+    import torch
+    for _ in range(2):
+        G = (A.T @ A).cpu().numpy()
+        try:
+            L = np.linalg.cholesky(G)
+        except np.linalg.LinAlgError:
+            q, _ = np.linalg.qr(A.cpu().numpy())
+            return torch.as_tensor(q, device=A.device)
+        Rinv = np.linalg.inv(L.T)
+        A = A @ torch.as_tensor(Rinv, dtype=A.dtype, device=A.device)
+    return A
+
+
+def reference_pca(x, mu, n_components, seed=58951, n_oversamples=10, sparse=None):
+    """The reference's local PCA of the stacked cells ``x`` (cells x genes, FP64
+    tensor, gene means ``mu``): scikit-learn's PCA(n_components,
+    random_state=seed) fitted on the double-centred genes x cells matrix.
+    Returns (coordinates: cells x k = components_.T, singular values: k, solver).
+    Any device."""
+    import torch
+    n, p = x.shape
+    k = int(n_components)
+    solver = sklearn_pca_solver(p, n, k)
+    if solver != 'randomized':
+        return None, None, solver
+    T = _Centred(x, mu, sparse)
+    r = k + n_oversamples
+    n_iter = 7 if k < 0.1 * min(p, n) else 4
+    transpose = p < n            # scikit-learn works on M = data^T = T when there are more cells than genes
+    mul, tmul = (T.t_mul, T.tt_mul) if transpose else (T.tt_mul, T.t_mul)
+    cols = p if transpose else n
+    Q = torch.as_tensor(np.random.RandomState(seed).normal(size=(cols, r)), dtype=x.dtype, device=x.device)
+    for _ in range(n_iter):
+        Q = _orthonormal(mul(Q))
+        Q = _orthonormal(tmul(Q))
+    Q = _orthonormal(mul(Q))
+    B = tmul(Q).T                # r x cols = Q^T M
+    Uh, s, Vt = np.linalg.svd(B.cpu().numpy(), full_matrices=False)
+    if transpose:
+        comp = Q @ torch.as_tensor(Uh[:, :k], dtype=x.dtype, device=x.device)     # cells x k
+    else:
+        comp = torch.as_tensor(Vt[:k].T.copy(), dtype=x.dtype, device=x.device)  # cells x k
+    return _largest_entry_positive(comp), torch.as_tensor(s[:k], dtype=x.dtype, device=x.device), solver
+
+
+def _largest_entry_positive(comp):
+    """scikit-learn's sign convention for components (columns here): the entry of
+    largest magnitude of each is positive."""
+    import torch
+    i = torch.argmax(comp.abs(), dim=0)
+    sign = torch.sign(comp[i, torch.arange(comp.shape[1], device=comp.device)])
+    return comp * torch.where(sign == 0, torch.ones_like(sign), sign)[None, :]
+
+
+def compute_pca(m1, m2, n_components, solver='exact'):
     """Returns ``(pca_1, pca_2, singular_values, mean_shift)`` as device tensors
-    (FP64): pca_k are the components_.T rows of each day."""
+    (FP64): pca_k are the components_.T rows of each day. ``solver`` 'exact'
+    decomposes the double-centred matrix exactly; 'reference' reproduces the
+    reference's scikit-learn PCA (its randomized solver where scikit-learn
+    picks that one, else the exact decomposition its full solvers compute)."""
     torch = N.require_cuda()
     x = torch.cat([torch.as_tensor(dense(m1), device='cuda', dtype=torch.float64),
                    torch.as_tensor(dense(m2), device='cuda', dtype=torch.float64)])
     mean_shift = x.mean(dim=0)
     n_components = min(int(n_components), x.shape[0])
+    n1 = m1.shape[0]
+    if solver not in ('exact', 'reference'):
+        raise ValueError("PCA solver must be 'exact' or 'reference'")
+    if solver == 'reference':
+        comp, s, _ = reference_pca(x, mean_shift, n_components)
+        if comp is not None:
+            return comp[:n1], comp[n1:], s, mean_shift
     gram = centred_gram(x, mean_shift)        # genes x genes, FP64 on the device
     # the eigendecomposition of this small (genes x genes) matrix runs in NumPy
     evals, evecs = np.linalg.eigh(gram.cpu().numpy())
@@ -72,5 +205,6 @@ def compute_pca(m1, m2, n_components):
     # V = Xc^T U S^-1 with Xc^T = (x - mean_shift) H: H U = U (U spans the range of a
     # matrix whose rows and columns sum to zero), so V = (x U - mean_shift . U) S^-1
     comp = (x @ U - (mean_shift @ U)[None, :]) / torch.where(s > 0, s, torch.ones_like(s))
-    n1 = m1.shape[0]
+    if solver == 'reference':
+        comp = _largest_entry_positive(comp)
     return comp[:n1], comp[n1:], s, mean_shift
