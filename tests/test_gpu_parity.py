@@ -279,3 +279,20 @@ def test_lse_matvec_primitive():
         m = x.max(axis=1)
         ref = (m + np.log2(np.exp2(x - m[:, None]).sum(axis=1))) * np.log(2.0)
         np.testing.assert_allclose(L.cpu().numpy(), ref, rtol=0, atol=2e-5)
+
+
+def test_otmodel_reference_pca_reproduces_the_reference_map(pair_golden):
+    """OTModel(pca='reference').compute_transport_map from the raw expression
+    matrix (device PCA as scikit-learn computes it, device cost and solve)
+    against the reference's own map of the golden pair (made by the reference's
+    code from the same matrix): coupling within COUPLING_TOL, marginals within
+    MARGINAL_TOL."""
+    import wot_gb300 as wot
+    z = pair_golden
+    X, day, growth = z['X'], z['day'], z['growth']
+    ids = np.array(['c%d' % i for i in range(len(day))])
+    ds = wot.Dataset(X, wot.Frame({'day': day, 'cell_growth_rate': growth}, index=ids))
+    tm = wot.OTModel(ds, pca='reference').compute_transport_map(0, 1)
+    ref = z['tmap_dg_default']
+    assert coupling_err(tm.X, ref) <= COUPLING_TOL
+    assert marginal_err(tm.X, ref) <= MARGINAL_TOL

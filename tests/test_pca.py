@@ -92,3 +92,14 @@ def test_oracle_pipeline_with_the_reference_pca(golden):
     a, b, s, _, _ = oom.compute_pca_reference(m0, m1, 30)
     C = oom.compute_default_cost_matrix(a, b, np.diag(s))
     np.testing.assert_allclose(C, golden['C'], rtol=0, atol=1e-10)
+
+
+def test_oracle_pipeline_reproduces_the_reference_map(golden):
+    """From the raw expression matrix: the oracle's compute_single_transport_map
+    with the reference's PCA gives the reference's own transport map
+    (tmap_dg_default of the golden pair, made by the reference's code) to 1e-12."""
+    from oracle import ot_model as oom
+    tm, _ = oom.compute_single_transport_map(golden['X'], golden['day'], 0.0, 1.0, growth=golden['growth'],
+                                             pca='reference')
+    ref = golden['tmap_dg_default']
+    assert np.abs(tm - ref).max() <= 1e-12 * np.abs(ref).max()
