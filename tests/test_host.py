@@ -47,6 +47,13 @@ def test_params_mapping_and_tau_none():
 
 def test_parse_configuration(tmp_path):
     assert parse_configuration(None) is None
+    # inline tables (wot/io/io.py:553-555: ',' between fields, ';' between rows) and header-less pairs
+    assert parse_configuration('t0,t1,epsilon;0,1,0.05;1,2,0.1') == {(0, 1): {'epsilon': 0.05},
+                                                                      (1, 2): {'epsilon': 0.1}}
+    assert parse_configuration('t0,t1;0,2;2,4') == {(0, 2): {}, (2, 4): {}}
+    bare = tmp_path / 'day_pairs.txt'
+    bare.write_text('0\t2\n2\t4\n')
+    assert parse_configuration(str(bare)) == {(0, 2): {}, (2, 4): {}}
     cfg = parse_configuration.__globals__['parse_per_timepair_configuration'](
         {(0, 1): {'epsilon': 0.1, 'lambda1': 2, 'junk': 5}})
     assert cfg == {(0, 1): {'epsilon': 0.1, 'lambda1': 2}}

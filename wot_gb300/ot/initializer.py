@@ -83,12 +83,22 @@ def parse_parameter_file(path):
     return result
 
 
-def read_day_pairs(path):
-    """Day-pair table file (wot.io.read_day_pairs) as a list-of-records table."""
+def read_day_pairs(spec):
+    """Day-pair table (wot/io/io.py:548-556) as a list-of-records table: a file
+    (separator sniffed), or an inline table with ',' between fields and ';'
+    between rows, e.g. 't0,t1,epsilon;0,1,0.05;1,2,0.1'. A table without a
+    t / t0 / t1 header row is read as (t0, t1) pairs."""
+    import os
     from ..dataset import Frame
-    with open(path) as f:
-        lines = [ln.rstrip('\n') for ln in f if ln.strip()]
-    sep = '\t' if '\t' in lines[0] else (',' if ',' in lines[0] else None)
+    if os.path.isfile(spec):
+        with open(spec) as f:
+            lines = [ln.rstrip('\n') for ln in f if ln.strip()]
+        sep = '\t' if '\t' in lines[0] else (',' if ',' in lines[0] else None)
+    else:
+        lines = [r.strip() for r in str(spec).split(';') if r.strip()]
+        sep = ','
+    if not lines:
+        raise ValueError('empty day-pair table')
     header = lines[0].split(sep)
     if not any(h in ('t', 't0', 't1') for h in header):
         header = ['t0', 't1']
