@@ -270,3 +270,35 @@ def test_otmodel_configuration_without_a_gpu(tmp_path, caplog):
     p0, p1 = m.select_pair({'t0': 0, 't1': 1, 'covariate': None})
     assert p0.X.base is not None and np.shares_memory(p0.X, m.matrix.X)
     assert p0.shape == (4, 5) and p1.shape == (4, 5)
+
+
+def test_objective_helpers_match_the_reference_forms():
+    """wot.ot.fdiv / fdivstar / primal / dual (optimal_transport.py:37-62): the
+    device code (run here on CPU tensors) equals the oracle's NumPy restatement,
+    zeros of R included; the public functions need a CUDA device."""
+    import torch
+    from oracle import optimal_transport as oot
+    from wot_gb300.ot import optimal_transport as wot_ot
+    rng = np.random.default_rng(3)
+    I, J, eps, l1, l2 = 7, 9, 0.05, 1.0, 50.0
+    C = rng.random((I, J))
+    K = np.exp(-C / eps)
+    a, b = rng.random(I) + 0.5, rng.random(J) + 0.5
+    R = (K.T * a).T * b
+    R[2, 3] = 0.0
+    dx, dy = np.ones(I) / I, np.ones(J) / J
+    p = rng.random(I) + 0.1
+    q = np.ones(J) * p.mean()
+    T = {k: torch.tensor(v) for k, v in dict(C=C, K=K, R=R, dx=dx, dy=dy, p=p, q=q, a=a, b=b).items()}
+    ref_p = oot.primal(C, K, R, dx, dy, p, q, a, b, eps, l1, l2)
+    ref_d = oot.dual(C, K, R, dx, dy, p, q, a, b, eps, l1, l2)
+    got_p = float(wot_ot._primal(T['C'], T['K'], T['R'], T['dx'], T['dy'], T['p'], T['q'], eps, l1, l2))
+    got_d = float(wot_ot._dual(T['K'], T['R'], T['dx'], T['dy'], T['p'], T['q'], T['a'], T['b'], eps, l1, l2))
+    assert abs(got_p - ref_p) <= 1e-13 * abs(ref_p) and abs(got_d - ref_d) <= 1e-13 * abs(ref_d)
+    x = R @ dy
+    assert abs(float(wot_ot._fdiv(l1, T['R'] @ T['dy'], T['p'], T['dx'])) - oot.fdiv(l1, x, p, dx)) <= 1e-14
+    u = rng.normal(size=I)
+    assert abs(float(wot_ot._fdivstar(l1, torch.tensor(u), T['p'], T['dx'])) - oot.fdivstar(l1, u, p, dx)) <= 1e-14
+    if not torch.cuda.is_available():
+        with pytest.raises(RuntimeError, match='CUDA device'):
+            wot_gb300.ot.primal(C, K, R, dx, dy, p, q, a, b, eps, l1, l2)

@@ -89,3 +89,64 @@ def compute_transport_matrix(solver, **params):
     # the first entry is the caller's G itself in the reference
     learned[0] = params['G']
     return tmap, learned
+
+
+# --- the objectives of the duality-gap test (optimal_transport.py:37-62) -------
+# The solvers evaluate these in O(I+J) on the device from their own state; these
+# functions give the reference's dense forms for arrays a caller holds. Inputs go
+# to the device in FP64; each returns a Python float.
+
+def _dev(x, torch):
+    if isinstance(x, torch.Tensor):
+        return x.to(dtype=torch.float64)
+    return torch.as_tensor(np.asarray(x, dtype=np.float64), device='cuda')
+
+
+def _fdiv(l, x, p, dx):
+    import torch
+    return l * torch.sum(dx * (x * torch.log(x / p) - x + p))
+
+
+def _fdivstar(l, u, p, dx):
+    import torch
+    return l * torch.sum((p * dx) * (torch.exp(u / l) - 1))
+
+
+def _primal(C, K, R, dx, dy, p, q, epsilon, lambda1, lambda2):
+    import torch
+    I, J = p.shape[0], q.shape[0]
+    return (_fdiv(lambda1, R @ dy, p, dx) + _fdiv(lambda2, R.T @ dx, q, dy)
+            + (epsilon * torch.sum(R * torch.nan_to_num(torch.log(R)) - R + K) + torch.sum(R * C)) / (I * J))
+
+
+def _dual(K, R, dx, dy, p, q, a, b, epsilon, lambda1, lambda2):
+    import torch
+    I, J = p.shape[0], q.shape[0]
+    return (-_fdivstar(lambda1, -epsilon * torch.log(a), p, dx) - _fdivstar(lambda2, -epsilon * torch.log(b), q, dy)
+            - epsilon * torch.sum(R - K) / (I * J))
+
+
+def fdiv(l, x, p, dx):
+    """KL-type divergence term (optimal_transport.py:37-38)."""
+    torch = N.require_cuda()
+    return float(_fdiv(l, _dev(x, torch), _dev(p, torch), _dev(dx, torch)))
+
+
+def fdivstar(l, u, p, dx):
+    """Its convex conjugate (optimal_transport.py:41-42)."""
+    torch = N.require_cuda()
+    return float(_fdivstar(l, _dev(u, torch), _dev(p, torch), _dev(dx, torch)))
+
+
+def primal(C, K, R, dx, dy, p, q, a, b, epsilon, lambda1, lambda2):
+    """Primal objective of the unbalanced problem (optimal_transport.py:45-53)."""
+    torch = N.require_cuda()
+    C, K, R, dx, dy, p, q = (_dev(v, torch) for v in (C, K, R, dx, dy, p, q))
+    return float(_primal(C, K, R, dx, dy, p, q, epsilon, lambda1, lambda2))
+
+
+def dual(C, K, R, dx, dy, p, q, a, b, epsilon, lambda1, lambda2):
+    """Dual objective (optimal_transport.py:56-62)."""
+    torch = N.require_cuda()
+    K, R, dx, dy, p, q, a, b = (_dev(v, torch) for v in (K, R, dx, dy, p, q, a, b))
+    return float(_dual(K, R, dx, dy, p, q, a, b, epsilon, lambda1, lambda2))
