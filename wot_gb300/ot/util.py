@@ -208,3 +208,30 @@ def compute_pca(m1, m2, n_components, solver='exact'):
     if solver == 'reference':
         comp = _largest_entry_positive(comp)
     return comp[:n1], comp[n1:], s, mean_shift
+
+
+class FittedPCA:
+    """The attributes of the reference's fitted scikit-learn PCA that its callers
+    read (ot_model.py:302 takes ``singular_values_``): ``components_`` (k x cells),
+    ``singular_values_`` (k), ``n_components_``, ``mean_`` (the per-cell mean over
+    genes that scikit-learn removed), all host FP64 arrays."""
+
+    def __init__(self, components, singular_values, mean):
+        self.components_ = components
+        self.singular_values_ = singular_values
+        self.n_components_ = int(singular_values.shape[0])
+        self.mean_ = mean
+
+
+def compute_pca_reference_api(m1, m2, n_components, solver='exact'):
+    """``wot.ot.compute_pca`` with the reference's return values (wot/ot/util.py:
+    240-255): ``(pca_1, pca_2, pca, mean_shift)`` as host arrays, ``pca`` a
+    FittedPCA. Computed on the device by ``compute_pca`` (``solver`` as there)."""
+    torch = N.require_cuda()
+    a, b, s, mean_shift = compute_pca(m1, m2, n_components, solver=solver)
+    comp = torch.cat([a, b])
+    x = torch.cat([torch.as_tensor(dense(m1), device='cuda', dtype=torch.float64),
+                   torch.as_tensor(dense(m2), device='cuda', dtype=torch.float64)])
+    cell_mean = (x - mean_shift[None, :]).mean(dim=1)
+    pca = FittedPCA(comp.T.cpu().numpy(), s.cpu().numpy(), cell_mean.cpu().numpy())
+    return a.cpu().numpy(), b.cpu().numpy(), pca, mean_shift.cpu().numpy()
