@@ -266,6 +266,15 @@ def test_otmodel_configuration_without_a_gpu(tmp_path, caplog):
     pairs = wot.OTModel(ds, config=str(cf))
     with pytest.raises(ValueError, match='not present in day_pairs'):
         pairs.compute_transport_map(1, 2)
+    # covariate pairs and covariate-restricted selection (ot_model.py:116-122, 271-292)
+    cv = np.array(['a', 'b', 'a', 'b', 'a', 'a', 'b', 'b', 'a', 'b', 'a', 'a'])
+    dsc = Dataset(ds.X, Frame({'day': day, 'covariate': cv}, index=ids), ds.var)
+    mc = wot.OTModel(dsc)
+    assert sorted(mc.get_covariate_pairs()) == [('a', 'a'), ('a', 'b'), ('b', 'a'), ('b', 'b')]
+    q0, q1 = mc.select_pair({'t0': 0, 't1': 1, 'covariate': ('b', 'a')})
+    assert list(q0.obs.index) == ['c1', 'c3'] and list(q1.obs.index) == ['c4', 'c5']
+    with pytest.raises(ValueError, match='Covariate'):
+        list(m.get_covariate_pairs())
     # contiguous day rows are selected as views of X
     p0, p1 = m.select_pair({'t0': 0, 't1': 1, 'covariate': None})
     assert p0.X.base is not None and np.shares_memory(p0.X, m.matrix.X)
