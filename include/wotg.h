@@ -4,8 +4,7 @@
  * The reference (wot 1.0.8) is pure Python/NumPy; it has no FFI of its own.
  * Each entry point below replaces one NumPy-level operation or Python function
  * of the reference's transport-map path, cited as file:line inside the
- * reference project, and is what a ctypes / cffi binding of that path binds
- * (see INTEGRATION.md for the binding).
+ * reference project, and is what a ctypes / cffi binding of that path binds.
  *
  * Conventions
  *  - All array arguments are DEVICE pointers owned by the caller; the library
@@ -164,11 +163,14 @@ int wotg_refine_potentials(const wotg_problem* problem, const wotg_params* param
  * in the reference. Same inputs, outputs and results; the solver's scratch comes
  * from a static 32 MiB device array (wotg_noalloc_scratch_bytes()) held by every
  * device that loads the library until exit, instead of a caller workspace.
- * Problems whose wotg_solve_workspace_bytes() exceeds it return WOTG_TOO_LARGE
- * (message in wotg_last_error()). The first call on each device looks up the
- * array's device address (cudaGetSymbolAddress); make it before any stream
- * capture. Calls that overlap on the GPU share the array and race: serialise them.
- * Allocates nothing. */
+ * Problems whose wotg_problem_workspace_bytes() exceeds it return WOTG_TOO_LARGE
+ * (message in wotg_last_error()); invalid problems return WOTG_BADARG as the
+ * workspace entry point does. The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress) and caches it for the life of
+ * the process; make that call before any stream capture, and make no call
+ * after cudaDeviceReset (the cached address does not survive a reset of the
+ * device's context). Calls that overlap on the GPU share the array and race:
+ * serialise them. Allocates nothing. */
 size_t wotg_noalloc_scratch_bytes(void);
 int wotg_compute_transport_matrix_noalloc(const wotg_problem* problem, const wotg_params* params,
                                           double* tmap, double* learned_growth, double* row_sums,
@@ -194,6 +196,20 @@ size_t wotg_lse_points_workspace_bytes(int64_t I, int64_t J, int32_t d);
 int wotg_lse_points(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy, int32_t d,
                     double scale, const double* w, double* L, void* workspace, size_t workspace_bytes,
                     void* stream);
+
+/* wotg_lse_points with each of the tensor-core kernel's mbarrier waits bounded
+ * to wait_tries tries (each suspends up to 1 us; wotg_lse_points and the
+ * solvers use 4,000,000, about 4 s; wait_tries <= 4,000,000). No counterpart in
+ * the reference, which has no device waits: this is the failure path of the
+ * on-the-fly half-step made testable. A wait that runs out makes the kernel
+ * stop issuing work, wait for every bulk copy and tensor-core product it has
+ * issued to finish (with the full budget), free its tensor memory and return;
+ * the call then returns WOTG_CUDA_ERROR with a message in wotg_last_error()
+ * and the device stays usable. With wait_tries = 0 every wait runs out at once.
+ * Synchronises the stream (to read the kernel's error word). */
+int wotg_lse_points_bounded(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy,
+                            int32_t d, double scale, const double* w, double* L, uint32_t wait_tries,
+                            void* workspace, size_t workspace_bytes, void* stream);
 
 /* Diagnostic (no counterpart in the reference): the mean device time of the
  * tensor-core kernel of wotg_lse_points alone (no packing, no finish), over

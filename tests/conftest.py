@@ -7,6 +7,9 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:                 # tests/parity.py, the shared parity measures
+    sys.path.insert(0, HERE)
 
 GOLDEN = os.path.join(ROOT, 'tests', 'golden')
 

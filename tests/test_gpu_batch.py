@@ -1,8 +1,9 @@
 """Batched solves (wotg_solve_batched): every item against the single-problem
 driver on the same device cost (iteration counts within a batch or two,
-couplings to 1e-5) and against the oracle's FP64 solve (couplings to 1e-4,
-marginals to 1e-5); the multi-RHS half-step against an FP64 log-sum-exp; the
-implicit map's pull-back / push-forward against dense products.
+couplings to 1e-5) and against the oracle's FP64 solve (the parity bounds of
+tests/parity.py: couplings to 1e-4 normalised and elementwise, marginals to
+1e-6); the multi-RHS half-step against an FP64 log-sum-exp; the implicit map's
+pull-back / push-forward against dense products.
 """
 import ctypes
 import logging
@@ -10,13 +11,10 @@ import logging
 import numpy as np
 import pytest
 
+from parity import assert_parity, coupling_err
+
 pytestmark = pytest.mark.gpu
 
-COUPLING_TOL = 1e-4
-# Marginals: the FP32 cost puts a relative error of about kappa C 2^-24 on each
-# exponent (1e-5 at eps = 0.025), which averages to ~1e-6 in the row and column
-# sums; the bound is the one the single-problem tests use.
-MARGINAL_TOL = 1e-5
 SAME_DEVICE_TOL = 1e-5
 DEFAULTS = dict(growth_iters=1, epsilon=0.05, lambda1=1, lambda2=50, epsilon0=1, tau=10000, scaling_iter=3000,
                 inner_iter_max=50, tolerance=1e-8, max_iter=1e7, batch_size=5, extra_iter=1000)
@@ -29,16 +27,6 @@ def built():
     assert torch.cuda.is_available()
     _build.build()
     _native.load()
-
-
-def coupling_err(T, R):
-    return np.abs(T - R).max() / np.abs(R).max()
-
-
-def marginal_err(T, R):
-    r = np.abs(T.sum(1) - R.sum(1)).max() / np.abs(R.sum(1)).max()
-    c = np.abs(T.sum(0) - R.sum(0)).max() / np.abs(R.sum(0)).max()
-    return max(r, c)
 
 
 def _pair(I, J, seed, d=30):
@@ -156,8 +144,7 @@ def test_batched_vs_oracle():
         ref = oot.compute_transport_matrix(solver=oot.optimal_transport_duality_gap, C=C, G=g, stats=st, **cfg)
         R = ref[0]
         T = m.dense().cpu().numpy()
-        assert coupling_err(T, R) <= COUPLING_TOL, cfg
-        assert marginal_err(T, R) <= MARGINAL_TOL, cfg
+        assert_parity(T, R, what=cfg)
 
 
 def test_implicit_map_pull_back_push_forward():

@@ -88,8 +88,63 @@ def test_find_path():
     tp = [0, 1, 2, 3, 4]
     assert find_path(0, 3, None, tp) == [(0, 1), (1, 2), (2, 3)]
     assert find_path(0, 4, [(0, 2), (2, 4), (0, 1), (1, 2)], tp) == [(0, 1), (1, 2), (2, 4)]
-    with pytest.raises(ValueError):
+    with pytest.raises(ValueError, match='not reachable'):
         find_path(0, 3, [(0, 1), (1, 2)], tp)
+    with pytest.raises(ValueError, match='must be present'):
+        find_path(0, 7, [(0, 1)], tp)
+    # ties: of two chains of the same length into a day, the one through the earlier predecessor is kept
+    assert find_path(0, 3, [(0, 1), (1, 3), (0, 2), (2, 3)], tp) == [(0, 1), (1, 3)]
+    assert find_path(0, 4, [(2, 4), (0, 2), (0, 1), (1, 4), (3, 4), (0, 3)], tp) == [(0, 1), (1, 4)]
+    assert find_path(0, 4, [(0, 1), (1, 2), (0, 2), (2, 4), (1, 3), (3, 4)], tp) == [(0, 1), (1, 2), (2, 4)]
+    # a longer chain starting at a day that t0 does not reach does not count
+    assert find_path(0, 3, [(0, 3), (1, 2), (2, 3)], tp) == [(0, 3)]
+
+
+def _longest_chain_length(t0, t1, pairs):
+    """Brute force: edges of the longest chain of forward pairs from t0 to t1."""
+    best = -1
+    stack = [(t0, 0)]
+    while stack:
+        day, n = stack.pop()
+        if day == t1:
+            best = max(best, n)
+        stack += [(b, n + 1) for a, b in pairs if a == day and a < b]
+    return best
+
+
+def test_find_path_matches_reference_cases():
+    """The reference's own find_path on 400 seeded pair sets
+    (tests/golden/make_paths.py): the same path wherever the reference returns
+    one, the same ValueError wherever it raises one; where the reference fails
+    with a KeyError (a longest chain into t1 that starts at a day t0 cannot
+    reach), the longest chain from t0, checked by brute force, or the
+    reference's ValueError when no chain from t0 reaches t1."""
+    import json
+    with open(os.path.join(ROOT, 'tests', 'golden', 'find_path_cases.json')) as f:
+        cases = json.load(f)
+    kinds = set()
+    for c in cases:
+        tp, t0, t1 = c['timepoints'], c['t0'], c['t1']
+        pairs = [tuple(p) for p in c['pairs']]
+        err = c.get('error')
+        kinds.add(err or 'path')
+        if err == 'ValueError':
+            with pytest.raises(ValueError):
+                find_path(t0, t1, pairs, tp)
+            continue
+        if err is None:
+            assert find_path(t0, t1, pairs, tp) == [tuple(p) for p in c['path']], c
+            continue
+        assert err == 'KeyError', c
+        if _longest_chain_length(t0, t1, pairs) <= 0:
+            with pytest.raises(ValueError, match='not reachable'):
+                find_path(t0, t1, pairs, tp)
+            continue
+        got = find_path(t0, t1, pairs, tp)
+        assert got[0][0] == t0 and got[-1][1] == t1 and all(p in pairs for p in got), c
+        assert all(a[1] == b[0] for a, b in zip(got[:-1], got[1:])), c
+        assert len(got) == _longest_chain_length(t0, t1, pairs), c
+    assert kinds == {'path', 'ValueError', 'KeyError'}
 
 
 def test_dataset_selection():
@@ -247,7 +302,7 @@ def test_otmodel_configuration_without_a_gpu(tmp_path, caplog):
     assert wot.OTModel(ds, solver='fixed_iters').solver is wot.ot.transport_stablev2
     with pytest.raises(ValueError, match='Unknown solver'):
         wot.OTModel(ds, solver='other')
-    assert wot.OTModel(ds).pca == 'exact' and wot.OTModel(ds, pca='reference').pca == 'reference'
+    assert wot.OTModel(ds).pca == 'reference' and wot.OTModel(ds, pca='exact').pca == 'exact'
     assert 'pca' not in wot.OTModel(ds, pca='reference').ot_config
     with pytest.raises(ValueError, match='pca'):
         wot.OTModel(ds, pca='randomized')

@@ -24,11 +24,20 @@ DEFAULTS = dict(growth_iters=2, epsilon=0.05, lambda1=1, lambda2=50, epsilon0=1,
 
 
 def _solve_both(lib, N, D, torch, C, G, cfg, solver, noalloc):
-    cost = D.cost_from_dense(C)
+    """C: a dense cost (materialised form), or a pair of point sets (x, y) whose
+    median-normalised squared distances are the cost (tensor-core form)."""
+    if isinstance(C, tuple):
+        cost = D.default_cost(*C)
+    else:
+        cost = D.cost_from_dense(C)
     I, J = cost.I, cost.J
     Gd = torch.as_tensor(np.asarray(G, dtype=np.float64), device='cuda')
     params = D.make_params(cfg, solver)
-    prob = N.Problem(I=I, J=J, C=cost.C.data_ptr(), ldc=cost.ldc, cost_scale=1.0, G=Gd.data_ptr())
+    prob = N.Problem(I=I, J=J, C=cost.C.data_ptr(), ldc=cost.ldc, cost_scale=float(cost.scale), G=Gd.data_ptr())
+    if isinstance(C, tuple):
+        prob.X, prob.ldx = cost.X.data_ptr(), cost.X.stride(0)
+        prob.Y, prob.ldy = cost.Y.data_ptr(), cost.Y.stride(0)
+        prob.d, prob.form = cost.X.shape[1], N.FORM_ONTHEFLY
     gi = params.growth_iters
     out = {'tmap': torch.empty((I, J), dtype=torch.float64, device='cuda'),
            'learned': torch.empty((gi, I), dtype=torch.float64, device='cuda'),
@@ -42,7 +51,7 @@ def _solve_both(lib, N, D, torch, C, G, cfg, solver, noalloc):
         st = lib.wotg_compute_transport_matrix_noalloc(ctypes.byref(prob), ctypes.byref(params), *ptrs,
                                                        ctypes.byref(stats), stream)
     else:
-        nbytes = lib.wotg_solve_workspace_bytes(I, J, cost.ldc)
+        nbytes = lib.wotg_problem_workspace_bytes(ctypes.byref(prob))
         ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
         st = lib.wotg_compute_transport_matrix(ctypes.byref(prob), ctypes.byref(params), *ptrs,
                                                ctypes.byref(stats), ws.data_ptr(), nbytes, stream)
@@ -66,10 +75,16 @@ def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(pair_golden)
     rng = np.random.default_rng(5)
     small_C = rng.random((37, 53)) * 2.0
     small_G = rng.lognormal(0, 0.3, 37)
+    # tensor-core form: packed point tiles, the error word, the redo counters and
+    # the exact-row list also live in the static array
+    pts = (rng.normal(size=(300, 30)).astype(np.float32), (rng.normal(size=(420, 30)) + 0.2).astype(np.float32))
+    pts_G = rng.lognormal(0, 0.3, 300)
     problems = [
         (z['C'], z['G'], dict(DEFAULTS), N.SOLVER_DUALITY_GAP),
         (z['C'], z['G'], dict(DEFAULTS), N.SOLVER_DUALITY_GAP),       # same problem again
+        (pts, pts_G, dict(DEFAULTS, growth_iters=1), N.SOLVER_DUALITY_GAP),
         (small_C, small_G, dict(DEFAULTS, growth_iters=1, scaling_iter=200, extra_iter=40), N.SOLVER_FIXED_ITERS),
+        (pts, pts_G, dict(DEFAULTS, growth_iters=1, epsilon=0.02), N.SOLVER_DUALITY_GAP),
     ]
     for C, G, cfg, solver in problems:
         st_a, ref, stats_a = _solve_both(lib, N, D, torch, C, G, cfg, solver, noalloc=False)
@@ -78,6 +93,7 @@ def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(pair_golden)
         for k in ref:
             assert _err(got[k], ref[k]) <= COUPLING_TOL, k
         assert stats_b['iterations'] == stats_a['iterations']
+        assert stats_b['exact_rows'] == stats_a['exact_rows']
     # and against the reference's own coupling for the golden pair
     params = ast.literal_eval(str(z['params_dg_default']))
     assert params == {}

@@ -14,7 +14,7 @@
 
 namespace wotg {
 
-constexpr uint32_t kTcWaitTries = 4000000;  // x up to 1 us per try: about 4 s
+constexpr uint32_t kTcWaitTries = kTcDefaultWaitTries;  // x up to 1 us per try: about 4 s
 
 // ---------------------------------------------------------------------------
 // Self-test of the MMA path: D (128 x 128, FP32) = A (128 x 32) B (128 x 32)^T
@@ -192,8 +192,13 @@ __global__ void tc_bias_pack_kernel(int64_t n, int64_t n_pad, const double* __re
 //               64 columns of half (w - 2) / 4 and folds them into a running
 //               (max, sum).
 // mbarriers hand buffers between roles (full / empty per B stage, per A buffer
-// and per accumulator). Every wait is bounded: a role that times out sets *err
-// and stops; the others then time out in turn, and TMEM is freed at the end.
+// and per accumulator). Every wait is bounded (wait_tries tries of up to 1 us):
+// a role that times out sets *err and a shared abort flag and stops, and the
+// other roles stop at their next wait. Before the CTA frees TMEM and exits,
+// whether it completed or gave up, the producer waits (with the full budget)
+// for every bulk copy it issued to land, and the MMA issuer commits once more
+// and waits until every MMA it issued has completed, so that no asynchronous
+// copy or product is still writing shared memory or TMEM when they are freed.
 // ---------------------------------------------------------------------------
 constexpr int kTcStages = 4;
 constexpr int kTcAcc = 2;            // TMEM accumulators (128 columns each)
@@ -215,8 +220,9 @@ struct TcSmem {
   static constexpr uint32_t kA = 0;                            // kABuf buffers
   static constexpr uint32_t kB = kABuf * kTileBytes;           // kStages buffers
   static constexpr uint32_t kBar = kB + kStages * kTileBytes;
-  // barriers: full[S], empty[S], a_full[kABuf], a_empty[kABuf], acc_full[kTcAcc], acc_empty[kTcAcc], TMEM slot
-  static constexpr uint32_t kBytes = kBar + 8 * (2 * kStages + 2 * kABuf + 2 * kTcAcc) + 16;
+  // barriers: full[S], empty[S], a_full[kABuf], a_empty[kABuf], acc_full[kTcAcc], acc_empty[kTcAcc],
+  // drain; then the TMEM slot and the abort flag
+  static constexpr uint32_t kBytes = kBar + 8 * (2 * kStages + 2 * kABuf + 2 * kTcAcc + 1) + 16;
   static constexpr uint32_t kAlloc = kBytes + 1024;            // slack for 1024-byte alignment
   static constexpr uint32_t kTmemCols = 128 * kTcAcc;
 };
@@ -290,7 +296,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
                                                                const __half* __restrict__ Qt,
                                                                int n_pt, int nq, float2* __restrict__ part,
                                                                const float* __restrict__ off,
-                                                               int* __restrict__ err) {
+                                                               int* __restrict__ err, uint32_t wait_tries) {
   using L = TcSmem<KP>;
   constexpr int S = L::kStages;
   extern __shared__ unsigned char smem_raw[];
@@ -303,7 +309,9 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
   uint64_t* a_empty = a_full + NA;
   uint64_t* acc_full = a_empty + NA;
   uint64_t* acc_empty = acc_full + kTcAcc;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + kTcAcc);
+  uint64_t* drain = acc_empty + kTcAcc;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t total = (int64_t)n_pt * nq;
   const int64_t f0 = tc_stretch_begin(blockIdx.x, total, gridDim.x);
@@ -330,6 +338,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
       tc::mbar_init(&acc_full[b], 1);
       tc::mbar_init(&acc_empty[b], kTcEpiWarps);
     }
+    tc::mbar_init(drain, 1);
+    *abort_flag = 0;
     tc::mbar_fence_init();
   }
   tc::fence_before_sync();
@@ -343,29 +353,47 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
     if (lane == 0) {
       // producer
       int t = t_first, q = q_first, seg = 0;
+      int j_last = -1, seg_last = -1;  // last column tile / row tile whose copy was issued
       for (int j = 0; j < n; ++j) {
         const int stage = j % S;
-        if (j >= S && !tc::mbar_wait(&empty[stage], (uint32_t)((j / S - 1) & 1), kTcWaitTries)) {
+        if (j >= S && !tc::mbar_wait_or_abort(&empty[stage], (uint32_t)((j / S - 1) & 1), wait_tries, abort_flag)) {
+          *abort_flag = 1;
           atomicExch(err, 1);
           break;
         }
         if (j == 0 || q == 0) {
           if (j > 0) ++seg;
-          if (seg >= NA && !tc::mbar_wait(&a_empty[seg % NA], (uint32_t)((seg / NA - 1) & 1), kTcWaitTries)) {
+          if (seg >= NA && !tc::mbar_wait_or_abort(&a_empty[seg % NA], (uint32_t)((seg / NA - 1) & 1), wait_tries,
+                                                    abort_flag)) {
+            *abort_flag = 1;
             atomicExch(err, 1);
             break;
           }
           tc::mbar_expect_tx(&a_full[seg % NA], L::kTileBytes);
           tc::bulk_g2s(sA + (uint32_t)(seg % NA) * L::kTileBytes, Pt + (int64_t)t * tile_halfs, L::kTileBytes,
                        &a_full[seg % NA]);
+          seg_last = seg;
         }
         tc::mbar_expect_tx(&full[stage], L::kTileBytes);
         tc::bulk_g2s(sB + (uint32_t)stage * L::kTileBytes, Qt + (int64_t)q * tile_halfs, L::kTileBytes,
                      &full[stage]);
+        j_last = j;
         if (++q == nq) {
           q = 0;
           ++t;
         }
+      }
+      // Drain: the last copy issued into each buffer has landed. Copies into one
+      // buffer complete its full barrier's phases in order and no later phase is
+      // armed, so these waits return at once for copies that the MMA issuer
+      // already consumed.
+      for (int b = 0; b < S && b <= j_last; ++b) {
+        const int jb = j_last - (j_last - b) % S;
+        if (!tc::mbar_wait(&full[b], (uint32_t)((jb / S) & 1), kTcWaitTries)) atomicExch(err, 2);
+      }
+      for (int b = 0; b < NA && b <= seg_last; ++b) {
+        const int sb = seg_last - (seg_last - b) % NA;
+        if (!tc::mbar_wait(&a_full[b], (uint32_t)((sb / NA) & 1), kTcWaitTries)) atomicExch(err, 2);
       }
     }
   } else if (warp == 1) {
@@ -374,6 +402,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
       // so run one after another; tiles are therefore issued in pairs with their
       // MMAs interleaved, giving the tensor core two independent chains.
       int q = q_first, seg = 0;
+      bool issued = false;
       constexpr int kGroup = kTcAcc >= 4 ? 2 : 1;
       for (int j0 = 0; j0 < n; j0 += kGroup) {
         const int cnt = j0 + 1 < n ? kGroup : 1;
@@ -386,10 +415,13 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
           const int stage = j % S, b = j % kTcAcc;
           const bool new_seg = j == 0 || q == 0;
           if (new_seg && j > 0) ++seg;
-          if (new_seg) good = good && tc::mbar_wait(&a_full[seg % NA], (uint32_t)((seg / NA) & 1), kTcWaitTries);
-          good = good && tc::mbar_wait(&full[stage], (uint32_t)((j / S) & 1), kTcWaitTries);
+          if (new_seg)
+            good = good &&
+                   tc::mbar_wait_or_abort(&a_full[seg % NA], (uint32_t)((seg / NA) & 1), wait_tries, abort_flag);
+          good = good && tc::mbar_wait_or_abort(&full[stage], (uint32_t)((j / S) & 1), wait_tries, abort_flag);
           if (j >= kTcAcc)
-            good = good && tc::mbar_wait(&acc_empty[b], (uint32_t)((j / kTcAcc - 1) & 1), kTcWaitTries);
+            good = good && tc::mbar_wait_or_abort(&acc_empty[b], (uint32_t)((j / kTcAcc - 1) & 1), wait_tries,
+                                                  abort_flag);
           a_addr[u] = sA + (uint32_t)(seg % NA) * L::kTileBytes;
           b_addr[u] = sB + (uint32_t)stage * L::kTileBytes;
           d_addr[u] = tmem + (uint32_t)(128 * b);
@@ -398,10 +430,12 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
           seg_end[u] = j == n - 1 || q == 0;
         }
         if (!good) {
+          *abort_flag = 1;
           atomicExch(err, 1);
           break;
         }
         tc::fence_after_sync();
+        issued = true;
         constexpr uint32_t idesc = tc::idesc_f16_f32(128, 128);
         constexpr uint32_t sbo = KP * 16;
 #pragma unroll
@@ -425,6 +459,12 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
           if (seg_end[u]) tc::mma_commit(&a_empty[seg_of[u] % NA]);
         }
       }
+      // Drain: a last commit arrives once every MMA issued above has completed
+      // (and after the arrivals of the commits before it).
+      if (issued) {
+        tc::mma_commit(drain);
+        if (!tc::mbar_wait(drain, 0, kTcWaitTries)) atomicExch(err, 2);
+      }
     }
   } else {
     // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, columns of group (w - 2) / 4
@@ -436,10 +476,13 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
     if (off) m = off[(int64_t)t * 128 + row];
     for (int j = 0; j < n; ++j) {
       const int b = j % kTcAcc;
-      const bool good =
-          __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[b], (uint32_t)((j / kTcAcc) & 1), kTcWaitTries));
+      const bool good = __all_sync(
+          0xffffffffu, tc::mbar_wait_or_abort(&acc_full[b], (uint32_t)((j / kTcAcc) & 1), wait_tries, abort_flag));
       if (!good) {
-        if (lane == 0) atomicExch(err, 1);
+        if (lane == 0) {
+          *abort_flag = 1;
+          atomicExch(err, 1);
+        }
         break;
       }
       tc::fence_after_sync();
@@ -514,13 +557,15 @@ int tc_ctas_per_sm(int kp) {
 int tc_parts() { return kTcParts; }
 
 int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int kp, int ctas, float2* part,
-                  const float* off, int* err, cudaStream_t st) {
+                  const float* off, int* err, cudaStream_t st, uint32_t wait_tries) {
   if (kp == 32) {
     WOTG_CUDA(tc_set_smem_attr<32>());
-    lse_tc_kernel<32><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err);
+    lse_tc_kernel<32><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
+                                                                     wait_tries);
   } else if (kp == 64) {
     WOTG_CUDA(tc_set_smem_attr<64>());
-    lse_tc_kernel<64><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err);
+    lse_tc_kernel<64><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
+                                                                     wait_tries);
   } else {
     return WOTG_BADARG;
   }
@@ -597,17 +642,17 @@ extern "C" size_t wotg_lse_points_workspace_bytes(int64_t I, int64_t J, int32_t 
   return points_layout(b, I, J, d, P);
 }
 
-extern "C" int wotg_lse_points(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy,
-                               int32_t d, double scale, const double* w, double* L, void* workspace,
-                               size_t workspace_bytes, void* stream) {
+static int lse_points_run(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy, int32_t d,
+                          double scale, const double* w, double* L, void* workspace, size_t workspace_bytes,
+                          cudaStream_t st, uint32_t wait_tries, int** err_out) {
   if (!X || !Y || !w || !L || I <= 0 || J <= 0 || d < 1 || d > tc_max_dim() || ldx < d || ldy < d ||
       !(scale > 0))
     return WOTG_BADARG;
   if (!workspace || workspace_bytes < wotg_lse_points_workspace_bytes(I, J, d)) return WOTG_WORKSPACE;
-  cudaStream_t st = (cudaStream_t)stream;
   Bump b{reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255)), 0};
   PointsLayout P{};
   points_layout(b, I, J, d, P);
+  if (err_out) *err_out = P.err;
   const double sigma = std::sqrt(scale);
   WOTG_CUDA(cudaMemsetAsync(P.err, 0, sizeof(int), st));
   int s = tc_pack_points(X, I, ldx, d, P.kp, (float)(2.0 * kLog2e * sigma), 1, P.Xa, P.normX, st);
@@ -616,11 +661,37 @@ extern "C" int wotg_lse_points(const float* X, int64_t I, int64_t ldx, const flo
   if (s) return s;
   s = tc_pack_bias(J, w, nullptr, P.normY, 1.0, scale * kLog2e, d, P.kp, P.Yb, st);
   if (s) return s;
-  s = tc_lse_launch(P.Xa, P.n_xt, P.Yb, P.n_yt, P.kp, P.ctas, P.part, nullptr, P.err, st);
+  s = tc_lse_launch(P.Xa, P.n_xt, P.Yb, P.n_yt, P.kp, P.ctas, P.part, nullptr, P.err, st, wait_tries);
   if (s) return s;
   lse_points_finish_kernel<<<(unsigned)((I + 255) / 256), 256, 0, st>>>(I, P.n_yt, P.ctas, kTcParts, P.part,
                                                                         P.normX, scale, L, nullptr);
   WOTG_LAUNCHED();
+  return WOTG_OK;
+}
+
+extern "C" int wotg_lse_points(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy,
+                               int32_t d, double scale, const double* w, double* L, void* workspace,
+                               size_t workspace_bytes, void* stream) {
+  return lse_points_run(X, I, ldx, Y, J, ldy, d, scale, w, L, workspace, workspace_bytes, (cudaStream_t)stream,
+                        kTcWaitTries, nullptr);
+}
+
+extern "C" int wotg_lse_points_bounded(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J,
+                                       int64_t ldy, int32_t d, double scale, const double* w, double* L,
+                                       uint32_t wait_tries, void* workspace, size_t workspace_bytes, void* stream) {
+  if (wait_tries > kTcWaitTries) return WOTG_BADARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  int* err_dev = nullptr;
+  int s = lse_points_run(X, I, ldx, Y, J, ldy, d, scale, w, L, workspace, workspace_bytes, st, wait_tries, &err_dev);
+  if (s) return s;
+  int err = 0;
+  WOTG_CUDA(cudaMemcpyAsync(&err, err_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
+  WOTG_CUDA(cudaStreamSynchronize(st));
+  if (err) {
+    set_last_message(err == 1 ? "tensor-core half-step: a bounded wait ran out; the kernel stopped and drained"
+                              : "tensor-core half-step: a drain wait ran out");
+    return WOTG_CUDA_ERROR;
+  }
   return WOTG_OK;
 }
 

@@ -39,7 +39,10 @@ int tc_parts();
 // (ctas + n_ptiles) * 128 * tc_parts() float2.
 // off (optional, n_ptiles x 128 floats): speculative form, each row's partial
 // is (off_row, sum 2^(d - off_row)); NULL: exact running-maximum form.
+// wait_tries bounds each of the kernel's mbarrier waits (tries of up to 1 us);
+// a wait that runs out sets *err (see lse_tc_kernel).
+constexpr uint32_t kTcDefaultWaitTries = 4000000;
 int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int kp, int ctas, float2* part,
-                  const float* off, int* err, cudaStream_t st);
+                  const float* off, int* err, cudaStream_t st, uint32_t wait_tries = kTcDefaultWaitTries);
 
 }  // namespace wotg

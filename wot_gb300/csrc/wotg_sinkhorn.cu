@@ -27,6 +27,7 @@
 // The row sums with the current b are exactly the next iteration's first
 // half-step, so a gap check costs one row pass that the next iteration reuses.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1295,17 +1296,21 @@ extern "C" int wotg_refine_potentials(const wotg_problem* prob, const wotg_param
 // address is looked up once per device, on that device's first call, with
 // cudaGetSymbolAddress (host code cannot use the symbol itself: on the host it
 // names a stand-in, not device memory); make that first call before any stream
-// capture. All calls share the array: calls whose work overlaps on the GPU
-// (other streams, other host threads) race on it, so serialise them. The
-// solver re-initialises everything it reads from the scratch at the start of
-// each solve (state vectors, max slots, counters), so no clearing between
-// calls is needed.
+// capture. The looked-up address is cached per device for the life of the
+// process; it does not survive cudaDeviceReset (or any other teardown of the
+// device's primary context), after which this entry point must not be called
+// again in the process. All calls share the array: calls whose work overlaps
+// on the GPU (other streams, other host threads) race on it, so serialise
+// them. The solver re-initialises everything it reads from the scratch at the
+// start of each solve (state vectors, max slots, counters, the tensor-core
+// form's packed points and error word), so no clearing between calls is
+// needed.
 // ---------------------------------------------------------------------------
 namespace {
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 constexpr int kNoAllocMaxDevices = 64;
-void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+std::atomic<void*> g_noalloc_ptr[kNoAllocMaxDevices] = {};
 }  // namespace
 
 extern "C" size_t wotg_noalloc_scratch_bytes(void) { return kNoAllocScratchBytes; }
@@ -1316,9 +1321,11 @@ extern "C" int wotg_compute_transport_matrix_noalloc(const wotg_problem* prob, c
                                                      void* stream) {
   if (!prob || !params) return WOTG_BADARG;
   const int64_t I = prob->I, J = prob->J, ldc = prob->ldc;
-  if (I <= 0 || J <= 0 || ldc < J || (ldc & 3) || !prob->C || !prob->G) return WOTG_BADARG;
+  if (I <= 0 || J <= 0 || ldc < J || (ldc & 3) || !prob->C || !prob->G || tc_valid(prob) != WOTG_OK)
+    return WOTG_BADARG;
   const size_t need = wotg_problem_workspace_bytes(prob);
-  if (need == 0 || need > kNoAllocScratchBytes) {
+  if (need == 0) return WOTG_BADARG;
+  if (need > kNoAllocScratchBytes) {
     char msg[256];
     snprintf(msg, sizeof(msg),
              "wotg_compute_transport_matrix_noalloc: a %lld x %lld problem needs %zu bytes of scratch, "
@@ -1330,11 +1337,13 @@ extern "C" int wotg_compute_transport_matrix_noalloc(const wotg_problem* prob, c
   int dev = 0;
   WOTG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kNoAllocMaxDevices) return WOTG_BADARG;
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    WOTG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_ptr[dev] = p;
+  void* scratch = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (!scratch) {
+    // set-up, once per device with that device current (two threads racing here
+    // look up and store the same address)
+    WOTG_CUDA(cudaGetSymbolAddress(&scratch, g_noalloc_scratch));
+    g_noalloc_ptr[dev].store(scratch, std::memory_order_release);
   }
   return wotg_compute_transport_matrix(prob, params, tmap, learned_growth, row_sums, u_bar, v_bar, stats,
-                                       g_noalloc_ptr[dev], kNoAllocScratchBytes, stream);
+                                       scratch, kNoAllocScratchBytes, stream);
 }

@@ -68,16 +68,27 @@ __device__ __forceinline__ void mbar_fence_init() {
 // after `max_tries` unsuccessful tries (~max_tries us) it returns false, so a
 // wait can never hang the kernel.
 constexpr uint32_t kSuspendNs = 1000;
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
+      : "memory");
+  return done != 0;
+}
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_tries) {
-  const uint32_t addr = smem_u32(bar);
+  for (uint32_t t = 0; t < max_tries; ++t)
+    if (mbar_try(bar, parity)) return true;
+  return false;
+}
+// The same wait, which also gives up as soon as *abort is set (another role of
+// the CTA gave up, so the phase it waits for may never complete).
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t parity, uint32_t max_tries,
+                                                   const volatile int* abort) {
   for (uint32_t t = 0; t < max_tries; ++t) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(addr), "r"(parity), "r"(kSuspendNs)
-        : "memory");
-    if (done) return true;
+    if (mbar_try(bar, parity)) return true;
+    if (*abort) return false;
   }
   return false;
 }

@@ -41,11 +41,12 @@ class OTModel:
         ``ncounts``, ``ncells``, ``solver`` ('duality_gap' | 'fixed_iters'),
         ``parameters`` (2-column file), and any ot_config key. The GPU-only
         ``form`` ('auto' | 'materialized' | 'onthefly') picks how the cost is
-        read by the Sinkhorn half-steps, and ``pca`` ('exact' | 'reference') how
-        the local PCA is computed: the exact decomposition of the double-centred
-        matrix, or the reference's own scikit-learn PCA (randomized solver,
-        random_state 58951) reproduced to FP64 rounding; neither is part of
-        ot_config.
+        read by the Sinkhorn half-steps, and ``pca`` ('reference' | 'exact') how
+        the local PCA is computed: the reference's own scikit-learn PCA
+        (randomized solver, random_state 58951) reproduced to FP64 rounding (the
+        default, so that maps equal the reference's from the expression matrix
+        on), or the exact decomposition of the double-centred matrix that the
+        randomized solver approximates; neither is part of ot_config.
     """
 
     def __init__(self, matrix, day_field='day', covariate_field='covariate',
@@ -61,9 +62,9 @@ class OTModel:
         ncounts = kwargs.pop('ncounts', None)
         ncells = kwargs.pop('ncells', None)
         # GPU-only knobs, kept out of ot_config: 'auto' | 'materialized' | 'onthefly', and
-        # the local PCA: 'exact' decomposition, or 'reference' (scikit-learn's solver and seed)
+        # the local PCA: 'reference' (scikit-learn's solver and seed), or the 'exact' decomposition
         self.form = kwargs.pop('form', 'auto')
-        self.pca = kwargs.pop('pca', 'exact')
+        self.pca = kwargs.pop('pca', 'reference')
         if self.pca not in ('exact', 'reference'):
             raise ValueError("pca must be 'exact' or 'reference'")
         self.matrix = _filter(self.matrix, cell_filter, gene_filter)

@@ -4,7 +4,7 @@ The reference stacks both days' cells, removes the per-gene mean, and fits
 ``sklearn.decomposition.PCA(n_components, random_state=58951)`` on ``x.T``, so
 genes are the samples and cells the features; the cell coordinates are the
 rows of ``components_.T`` and ``singular_values_`` scale them in the cost.
-Here the same double-centred matrix is decomposed exactly: the (genes x genes)
+``solver='exact'`` decomposes the same double-centred matrix exactly: the (genes x genes)
 Gram matrix of the centred ``x.T`` is formed on the device in FP64, its small
 eigendecomposition runs in NumPy, and the top eigenpairs give the singular
 values and (projected on the device) the cell coordinates. The reference's
@@ -20,7 +20,7 @@ so only x^T x touches the cells. Expression matrices are mostly zeros
 product (cuSPARSE, FP64) over the nonzeros instead of a dense FP64 GEMM, about
 1/density times fewer FMAs on a part whose FP64 rate is low.
 
-``solver='reference'`` instead reproduces the reference's decomposition itself:
+``solver='reference'`` (the default) reproduces the reference's decomposition itself:
 scikit-learn's choice of solver for this shape and, where that is its
 randomized solver, the randomized range finder of Halko, Martinsson and Tropp
 (SIAM Review 53(2), 2011, Algorithm 4.4 with a re-orthonormalised power
@@ -178,12 +178,13 @@ def _largest_entry_positive(comp):
     return comp * torch.where(sign == 0, torch.ones_like(sign), sign)[None, :]
 
 
-def compute_pca(m1, m2, n_components, solver='exact'):
+def compute_pca(m1, m2, n_components, solver='reference'):
     """Returns ``(pca_1, pca_2, singular_values, mean_shift)`` as device tensors
-    (FP64): pca_k are the components_.T rows of each day. ``solver`` 'exact'
-    decomposes the double-centred matrix exactly; 'reference' reproduces the
-    reference's scikit-learn PCA (its randomized solver where scikit-learn
-    picks that one, else the exact decomposition its full solvers compute)."""
+    (FP64): pca_k are the components_.T rows of each day. ``solver``
+    'reference' (the default) reproduces the reference's scikit-learn PCA (its
+    randomized solver where scikit-learn picks that one, else the exact
+    decomposition its full solvers compute); 'exact' decomposes the
+    double-centred matrix exactly."""
     torch = N.require_cuda()
     x = torch.cat([torch.as_tensor(dense(m1), device='cuda', dtype=torch.float64),
                    torch.as_tensor(dense(m2), device='cuda', dtype=torch.float64)])
@@ -223,7 +224,7 @@ class FittedPCA:
         self.mean_ = mean
 
 
-def compute_pca_reference_api(m1, m2, n_components, solver='exact'):
+def compute_pca_reference_api(m1, m2, n_components, solver='reference'):
     """``wot.ot.compute_pca`` with the reference's return values (wot/ot/util.py:
     240-255): ``(pca_1, pca_2, pca, mean_shift)`` as host arrays, ``pca`` a
     FittedPCA. Computed on the device by ``compute_pca`` (``solver`` as there)."""
