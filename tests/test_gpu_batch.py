@@ -2,8 +2,9 @@
 driver on the same device cost (iteration counts within a batch or two,
 couplings to 1e-5) and against the oracle's FP64 solve (the parity bounds of
 tests/parity.py: couplings to 1e-4 normalised and elementwise, marginals to
-1e-6); the multi-RHS half-step against an FP64 log-sum-exp; the implicit map's
-pull-back / push-forward against dense products.
+the batched pass's BATCHED_MARGINAL_TOL); the multi-RHS half-step against an
+FP64 log-sum-exp; the implicit map's pull-back / push-forward against dense
+products.
 """
 import ctypes
 import logging
@@ -11,7 +12,7 @@ import logging
 import numpy as np
 import pytest
 
-from parity import assert_parity, coupling_err
+from parity import assert_parity_batched, coupling_err
 
 pytestmark = pytest.mark.gpu
 
@@ -144,7 +145,7 @@ def test_batched_vs_oracle():
         ref = oot.compute_transport_matrix(solver=oot.optimal_transport_duality_gap, C=C, G=g, stats=st, **cfg)
         R = ref[0]
         T = m.dense().cpu().numpy()
-        assert_parity(T, R, what=cfg)
+        assert_parity_batched(T, R, what=cfg)
 
 
 def test_implicit_map_pull_back_push_forward():

@@ -14,7 +14,8 @@ struct Coef {
   double lambda1, lambda2;
   double logI, logJ, logq, q;
   double kappa;             // cost_scale / eps
-  float kappa2;             // cost_scale / eps * log2(e)
+  float kappa2;             // cost_scale / eps * log2(e), rounded towards zero
+  float kappa2_lo;          // the remainder (> 0), so kappa2 + kappa2_lo carries ~48 bits
 };
 
 // The reference's exponents alpha1 = lambda1 / (lambda1 + eps) and
@@ -36,7 +37,16 @@ __host__ __device__ inline Coef make_coef(double eps, double lambda1, double lam
   c.q = q;
   c.logq = log(q);
   c.kappa = cost_scale / eps;
-  c.kappa2 = (float)(cost_scale / eps * 1.4426950408889634074);
+  // kappa2 = hi + lo with lo > 0: hi the FP32 value at or below the FP64 one, lo
+  // the FP32 remainder (a tiny positive value when hi is exact), so that
+  // -hi * inf - lo * inf of a +inf padding cost entry is -inf, never NaN
+  const double k2 = cost_scale / eps * 1.4426950408889634074;
+  float hi = (float)k2;
+  if ((double)hi > k2) hi = nextafterf(hi, 0.f);
+  float lo = (float)(k2 - (double)hi);
+  if (!(lo > 0.f)) lo = 1e-30f;
+  c.kappa2 = hi;
+  c.kappa2_lo = lo;
   return c;
 }
 

@@ -86,6 +86,43 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* slot, doub
   if (x > 0.0) atomicMax(slot, (unsigned long long)__double_as_longlong(x));
 }
 
+// ---------------------------------------------------------------------------
+// Precision of the streamed half-steps. The exponent of element (i, j) of a row
+// pass is w_j - kappa2 C_ij (base 2), whose terms are tens to hundreds while
+// the entries that carry mass have exponents within a few units of the row's
+// log-sum-exp. Rounding the weight or the exponent to FP32 at that magnitude
+// (|x| 2^-24) would put an error of ~1e-6 (1e-5 at eps = 0.01) on every entry,
+// which the iterations carry into the potentials. Instead:
+//  * a weight w (FP64) is kept as hi + lo: hi on a 2^-14 grid (exact in FP32
+//    for |w| < 512), lo the FP32 remainder;
+//  * each row (column) is summed relative to an offset o on the same grid, the
+//    previous half-step's log-sum-exp of that row, so that hi - o is exact;
+//  * kappa2 is split into hi + lo (Coef) and the exponent is
+//        x = fma(-k2hi, C, hi - o) + fma(-k2lo, C, lo),
+//    small for the entries that matter, rounded once; o is added back in FP64.
+// What remains is the FP32 storage of C itself.
+// ---------------------------------------------------------------------------
+constexpr double kWeightGrid = 16384.0;  // 2^14
+
+__device__ __forceinline__ void split_weight(double w, float* hi, float* lo, int64_t k) {
+  if (!(fabs(w) < 1e30)) {  // -inf (zero weight), +inf, NaN: carried by hi alone
+    hi[k] = (float)w;
+    lo[k] = 0.f;
+    return;
+  }
+  const float h = (float)(rint(w * kWeightGrid) / kWeightGrid);
+  hi[k] = h;
+  lo[k] = (float)(w - (double)h);
+}
+
+// x on the weight grid; 0 when x is not finite.
+__device__ __forceinline__ float grid_value(double x) {
+  return fabs(x) < 1e30 ? (float)(rint(x * kWeightGrid) / kWeightGrid) : 0.f;
+}
+// Base-2 grid offset of a row whose previous log-sum-exp (natural log) is L;
+// 0 when L is not finite.
+__device__ __forceinline__ float grid_offset(double L) { return grid_value(L * kLog2e); }
+
 struct Bump {
   char* base;
   size_t off;

@@ -50,8 +50,10 @@ struct Vecs {
   double* p;       // I
   double* Lrow;    // I   log sum_j exp(v_j/eps + lb_j - kappa C_ij)
   double* Lcol;    // J   log sum_i exp(u_i/eps + la_i - kappa C_ij)
-  float* wrow;     // I   (u_i/eps + la_i) * log2(e), FP32 operand of the column pass
-  float* wcol;     // ldc (v_j/eps + lb_j) * log2(e), zero in padding columns
+  float* wrow;     // I   (u_i/eps + la_i) * log2(e), FP32 operand of the column pass (hi part, see split_weight)
+  float* wcol;     // ldc (v_j/eps + lb_j) * log2(e), zero in padding columns (hi part)
+  float* wrow_lo;  // I   remainders of the weights (lo parts)
+  float* wcol_lo;  // ldc
   float2* part;    // nrb x ldc column-pass partials (m, s) in base 2
   unsigned long long* maxslot;  // 2 slots of max(a, b) bits, alternating per iteration
   double* red;     // kRedBlocks x kNq reduction partials
@@ -108,7 +110,7 @@ __device__ __forceinline__ double a_update(int64_t i, double L, const Vecs& V, c
   const double la_new = c.alpha1 * (V.logp[i] - logs) - ui * c.inv_l1e;
   V.la_old[i] = V.la[i];
   V.la[i] = la_new;
-  V.wrow[i] = (float)((ui * c.inv_eps + la_new) * kLog2e);
+  split_weight((ui * c.inv_eps + la_new) * kLog2e, V.wrow, V.wrow_lo, i);
   return exp(la_new);
 }
 
@@ -118,7 +120,7 @@ __device__ __forceinline__ double b_update(int64_t j, double L, const Vecs& V, c
   const double lb_new = c.alpha2 * (c.logq - logt) - vj * c.inv_l2e;
   V.lb_old[j] = V.lb[j];
   V.lb[j] = lb_new;
-  V.wcol[j] = (float)((vj * c.inv_eps + lb_new) * kLog2e);
+  split_weight((vj * c.inv_eps + lb_new) * kLog2e, V.wcol, V.wcol_lo, j);
   return exp(lb_new);
 }
 
@@ -136,9 +138,21 @@ __device__ __forceinline__ void block_max_to_slot(double v, unsigned long long* 
   }
 }
 
+// Exponent of one element: plain (w - k2 C, one rounding) or precise (relative
+// to the grid offset o with the weight's and kappa2's low parts, see
+// split_weight).
+template <bool PREC>
+__device__ __forceinline__ float expo(float cc, float w, float wl, float o, float k2, float k2l) {
+  if (PREC) return fmaf(-k2, cc, w - o) + fmaf(-k2l, cc, wl);
+  return fmaf(-k2, cc, w);
+}
+
 // Row pass: one warp per row, 128-bit streaming loads of C, online base-2 LSE.
 // UPDATE_A additionally applies the a-update to the row (first half-step).
-template <bool UPDATE_A>
+// PREC: the solver's precise form (weights hi + lo in V.wcol / V.wcol_lo, the
+// row's previous log-sum-exp in V.Lrow as its offset); otherwise the plain form
+// on one FP32 weight vector (the standalone half-step).
+template <bool UPDATE_A, bool PREC>
 __global__ void __launch_bounds__(256) row_pass_kernel(const float* __restrict__ C, Geom g,
                                                        Vecs V, Coef c, int parity) {
   const int lane = threadIdx.x & 31;
@@ -146,24 +160,28 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const float* __restrict__
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t nv = g.ldc >> 2;
   const float4* __restrict__ w4 = reinterpret_cast<const float4*>(V.wcol);
-  const float k2 = c.kappa2;
+  const float4* __restrict__ wl4 = reinterpret_cast<const float4*>(PREC ? V.wcol_lo : V.wcol);
+  const float k2 = c.kappa2, k2l = c.kappa2_lo;
   double amax = 0.0;
   for (int64_t i = warp; i < g.I; i += nwarps) {
     const float4* __restrict__ row = reinterpret_cast<const float4*>(C + i * g.ldc);
+    const float o = PREC ? grid_offset(V.Lrow[i]) : 0.f;
     float m = kNegBig, s = 0.f;
     int64_t k = lane;
     for (; k + 96 < nv; k += 128) {
-      float4 cc[4], ww[4];
+      float4 cc[4], ww[4], wl[4];
 #pragma unroll
       for (int t = 0; t < 4; ++t) cc[t] = ld_stream(row + k + 32 * t);
 #pragma unroll
       for (int t = 0; t < 4; ++t) ww[t] = __ldg(w4 + k + 32 * t);
 #pragma unroll
+      for (int t = 0; t < 4; ++t) wl[t] = PREC ? __ldg(wl4 + k + 32 * t) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
       for (int t = 0; t < 4; ++t) {
-        const float x0 = fmaf(-k2, cc[t].x, ww[t].x);
-        const float x1 = fmaf(-k2, cc[t].y, ww[t].y);
-        const float x2 = fmaf(-k2, cc[t].z, ww[t].z);
-        const float x3 = fmaf(-k2, cc[t].w, ww[t].w);
+        const float x0 = expo<PREC>(cc[t].x, ww[t].x, wl[t].x, o, k2, k2l);
+        const float x1 = expo<PREC>(cc[t].y, ww[t].y, wl[t].y, o, k2, k2l);
+        const float x2 = expo<PREC>(cc[t].z, ww[t].z, wl[t].z, o, k2, k2l);
+        const float x3 = expo<PREC>(cc[t].w, ww[t].w, wl[t].w, o, k2, k2l);
         const float mn = fmaxf(m, fmaxf(fmaxf(x0, x1), fmaxf(x2, x3)));
         s = s * ex2(m - mn) + ((ex2(x0 - mn) + ex2(x1 - mn)) + (ex2(x2 - mn) + ex2(x3 - mn)));
         m = mn;
@@ -172,17 +190,18 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const float* __restrict__
     for (; k < nv; k += 32) {
       const float4 cc = ld_stream(row + k);
       const float4 ww = __ldg(w4 + k);
-      const float x0 = fmaf(-k2, cc.x, ww.x);
-      const float x1 = fmaf(-k2, cc.y, ww.y);
-      const float x2 = fmaf(-k2, cc.z, ww.z);
-      const float x3 = fmaf(-k2, cc.w, ww.w);
+      const float4 wl = PREC ? __ldg(wl4 + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float x0 = expo<PREC>(cc.x, ww.x, wl.x, o, k2, k2l);
+      const float x1 = expo<PREC>(cc.y, ww.y, wl.y, o, k2, k2l);
+      const float x2 = expo<PREC>(cc.z, ww.z, wl.z, o, k2, k2l);
+      const float x3 = expo<PREC>(cc.w, ww.w, wl.w, o, k2, k2l);
       const float mn = fmaxf(m, fmaxf(fmaxf(x0, x1), fmaxf(x2, x3)));
       s = s * ex2(m - mn) + ((ex2(x0 - mn) + ex2(x1 - mn)) + (ex2(x2 - mn) + ex2(x3 - mn)));
       m = mn;
     }
     warp_lse(m, s);
     if (lane == 0) {
-      const double L = ((double)m + log2((double)s)) * kLn2;
+      const double L = ((double)o + (double)m + log2((double)s)) * kLn2;
       V.Lrow[i] = L;
       if (UPDATE_A) amax = fmax(amax, a_update(i, L, V, c));
     }
@@ -203,6 +222,13 @@ __global__ void a_update_kernel(Geom g, Vecs V, Coef c, int parity) {
 // writes one (m, s) base-2 LSE partial per column and row block.
 constexpr int kColRowChunk = 4;
 
+// Offset of column j of the precise column pass (0 in padding columns); the
+// combine recomputes the same value from the same V.Lcol.
+__device__ __forceinline__ float col_offset(const Vecs& V, const Geom& g, int64_t j) {
+  return j < g.J ? grid_offset(V.Lcol[j]) : 0.f;
+}
+
+template <bool PREC>
 __global__ void __launch_bounds__(256) col_partial_kernel(const float* __restrict__ C, Geom g,
                                                           Vecs V, Coef c) {
   const int64_t c4 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -210,24 +236,31 @@ __global__ void __launch_bounds__(256) col_partial_kernel(const float* __restric
   const int64_t r0 = (int64_t)blockIdx.y * g.rows_per;
   const int64_t r1 = min(g.I, r0 + g.rows_per);
   if (c4 >= nv) return;
-  const float k2 = c.kappa2;
+  const float k2 = c.kappa2, k2l = c.kappa2_lo;
+  float o[4] = {0.f, 0.f, 0.f, 0.f};
+  if (PREC) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = col_offset(V, g, c4 * 4 + q);
+  }
   float m[4] = {kNegBig, kNegBig, kNegBig, kNegBig};
   float s[4] = {0.f, 0.f, 0.f, 0.f};
   int64_t i = r0;
   for (; i + kColRowChunk <= r1; i += kColRowChunk) {
     float4 cc[kColRowChunk];
-    float w[kColRowChunk];
+    float w[kColRowChunk], wl[kColRowChunk];
 #pragma unroll
     for (int t = 0; t < kColRowChunk; ++t) cc[t] = ld_stream(reinterpret_cast<const float4*>(C + (i + t) * g.ldc) + c4);
 #pragma unroll
     for (int t = 0; t < kColRowChunk; ++t) w[t] = __ldg(V.wrow + i + t);
+#pragma unroll
+    for (int t = 0; t < kColRowChunk; ++t) wl[t] = PREC ? __ldg(V.wrow_lo + i + t) : 0.f;
     float x[4][kColRowChunk];
 #pragma unroll
     for (int t = 0; t < kColRowChunk; ++t) {
-      x[0][t] = fmaf(-k2, cc[t].x, w[t]);
-      x[1][t] = fmaf(-k2, cc[t].y, w[t]);
-      x[2][t] = fmaf(-k2, cc[t].z, w[t]);
-      x[3][t] = fmaf(-k2, cc[t].w, w[t]);
+      x[0][t] = expo<PREC>(cc[t].x, w[t], wl[t], o[0], k2, k2l);
+      x[1][t] = expo<PREC>(cc[t].y, w[t], wl[t], o[1], k2, k2l);
+      x[2][t] = expo<PREC>(cc[t].z, w[t], wl[t], o[2], k2, k2l);
+      x[3][t] = expo<PREC>(cc[t].w, w[t], wl[t], o[3], k2, k2l);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -245,7 +278,9 @@ __global__ void __launch_bounds__(256) col_partial_kernel(const float* __restric
   for (; i < r1; ++i) {
     const float4 cc = ld_stream(reinterpret_cast<const float4*>(C + i * g.ldc) + c4);
     const float w = __ldg(V.wrow + i);
-    const float xs[4] = {fmaf(-k2, cc.x, w), fmaf(-k2, cc.y, w), fmaf(-k2, cc.z, w), fmaf(-k2, cc.w, w)};
+    const float wl = PREC ? __ldg(V.wrow_lo + i) : 0.f;
+    const float xs[4] = {expo<PREC>(cc.x, w, wl, o[0], k2, k2l), expo<PREC>(cc.y, w, wl, o[1], k2, k2l),
+                         expo<PREC>(cc.z, w, wl, o[2], k2, k2l), expo<PREC>(cc.w, w, wl, o[3], k2, k2l)};
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const float mn = fmaxf(m[q], xs[q]);
@@ -260,17 +295,18 @@ __global__ void __launch_bounds__(256) col_partial_kernel(const float* __restric
 
 // Column pass, phase 2: merge the row-block partials of each column in FP64,
 // then (UPDATE_B) the reference's b-update.
-template <bool UPDATE_B>
+template <bool UPDATE_B, bool PREC>
 __global__ void col_combine_kernel(Geom g, Vecs V, Coef c, int parity) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double bmax = 0.0;
   if (j < g.J) {
+    const float o = PREC ? col_offset(V, g, j) : 0.f;
     float m = kNegBig, s = 0.f;
     for (int r = 0; r < g.nrb; ++r) {
       const float2 ps = V.part[(int64_t)r * g.ldc + j];
       lse_merge(m, s, ps.x, ps.y);
     }
-    const double L = ((double)m + log2((double)s)) * kLn2;
+    const double L = ((double)o + (double)m + log2((double)s)) * kLn2;
     V.Lcol[j] = L;
     if (UPDATE_B) bmax = b_update(j, L, V, c);
   }
@@ -289,13 +325,13 @@ __global__ void absorb_kernel(Geom g, Vecs V, Coef c, double tau, int parity) {
     const double un = V.u[idx] + c.eps * V.la[idx];
     V.u[idx] = un;
     V.la[idx] = 0.0;
-    V.wrow[idx] = (float)(un * c.inv_eps * kLog2e);
+    split_weight(un * c.inv_eps * kLog2e, V.wrow, V.wrow_lo, idx);
   } else if (idx < g.I + g.J) {
     const int64_t j = idx - g.I;
     const double vn = V.v[j] + c.eps * V.lb[j];
     V.v[j] = vn;
     V.lb[j] = 0.0;
-    V.wcol[j] = (float)(vn * c.inv_eps * kLog2e);
+    split_weight(vn * c.inv_eps * kLog2e, V.wcol, V.wcol_lo, j);
   }
 }
 
@@ -312,14 +348,14 @@ __global__ void rescale_kernel(Geom g, Vecs V, double eps_old, double inv_eps_ne
     V.u[idx] = un;
     V.la[idx] = 0.0;
     V.la_old[idx] = 0.0;
-    V.wrow[idx] = (float)(un * inv_eps_new * kLog2e);
+    split_weight(un * inv_eps_new * kLog2e, V.wrow, V.wrow_lo, idx);
   } else if (idx < g.I + g.J) {
     const int64_t j = idx - g.I;
     const double vn = V.v[j] + eps_old * V.lb[j];
     V.v[j] = vn;
     V.lb[j] = 0.0;
     V.lb_old[j] = 0.0;
-    V.wcol[j] = (float)(vn * inv_eps_new * kLog2e);
+    split_weight(vn * inv_eps_new * kLog2e, V.wcol, V.wcol_lo, j);
   }
 }
 
@@ -339,13 +375,17 @@ __global__ void init_kernel(Geom g, Vecs V, const double* __restrict__ G) {
     V.p[idx] = pi;
     V.logp[idx] = log(pi);
     V.wrow[idx] = 0.f;
+    V.wrow_lo[idx] = 0.f;
+    V.Lrow[idx] = 0.0;
   }
   if (idx < g.ldc) {
     V.wcol[idx] = 0.f;
+    V.wcol_lo[idx] = 0.f;
     if (idx < g.J) {
       V.v[idx] = 0.0;
       V.lb[idx] = 0.0;
       V.lb_old[idx] = 0.0;
+      V.Lcol[idx] = 0.0;
     }
   }
 }
@@ -358,13 +398,15 @@ __global__ void load_potentials_kernel(Geom g, Vecs V, const double* __restrict_
     V.u[idx] = ubar[idx];
     V.la[idx] = 0.0;
     V.la_old[idx] = 0.0;
-    V.wrow[idx] = (float)(ubar[idx] * inv_eps * kLog2e);
+    V.Lrow[idx] = 0.0;
+    split_weight(ubar[idx] * inv_eps * kLog2e, V.wrow, V.wrow_lo, idx);
   } else if (idx < g.I + g.J) {
     const int64_t j = idx - g.I;
     V.v[j] = vbar[j];
     V.lb[j] = 0.0;
     V.lb_old[j] = 0.0;
-    V.wcol[j] = (float)(vbar[j] * inv_eps * kLog2e);
+    V.Lcol[j] = 0.0;
+    split_weight(vbar[j] * inv_eps * kLog2e, V.wcol, V.wcol_lo, j);
   }
 }
 
@@ -516,17 +558,29 @@ __global__ void potentials_kernel(Geom g, Vecs V, Coef c, double* __restrict__ u
   }
 }
 
+// 2^t for an FP64 exponent t: the integer part exactly (as the FP64 exponent
+// field), the fraction by FP32 ex2 (relative error ~2^-22); 0 below 2^-1020,
+// NaN for NaN.
+__device__ __forceinline__ double exp2_split(double t) {
+  if (!(t > -1020.0)) return t != t ? t : 0.0;
+  if (t >= 1024.0) return INFINITY;
+  const double ti = floor(t);
+  const double scale = __longlong_as_double((long long)(ti + 1023.0) << 52);
+  return (double)ex2((float)(t - ti)) * scale;
+}
+
 // Dense coupling tmap_ij = a_i exp((u_i - C_ij + v_j)/eps) b_j * exp(log_scale), written
-// FP64 row-major (stride J) like the reference's ndarray.
+// FP64 row-major (stride J) like the reference's ndarray. The exponent is formed in
+// FP64 (its terms are tens to hundreds; only the fraction goes through FP32).
 __global__ void __launch_bounds__(256) coupling_kernel(const float* __restrict__ C, Geom g, Vecs V,
                                                        Coef c, double log_scale, double* __restrict__ out) {
-  const float k2 = c.kappa2;
+  const double k2 = c.kappa * kLog2e;
   for (int64_t i = blockIdx.y; i < g.I; i += gridDim.y) {
-    const float wr = (float)((V.u[i] * c.inv_eps + V.la[i] + log_scale) * kLog2e);
+    const double wr = (V.u[i] * c.inv_eps + V.la[i] + log_scale) * kLog2e;
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.J;
          j += (int64_t)gridDim.x * blockDim.x) {
-      const float x = wr + V.wcol[j] - k2 * C[i * g.ldc + j];
-      out[i * g.J + j] = (double)ex2(x);
+      const double wc = (V.v[j] * c.inv_eps + V.lb[j]) * kLog2e;
+      out[i * g.J + j] = exp2_split(wr + wc - k2 * (double)C[i * g.ldc + j]);
     }
   }
 }
@@ -728,12 +782,12 @@ struct Solver {
     if (lrow_valid) {
       a_update_kernel<<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, parity);
     } else {
-      row_pass_kernel<true><<<g.row_grid, 256, 0, st>>>(C, g, V, c, parity);
+      row_pass_kernel<true, true><<<g.row_grid, 256, 0, st>>>(C, g, V, c, parity);
     }
     WOTG_LAUNCHED();
-    col_partial_kernel<<<dim3(g.ncb, g.nrb), 256, 0, st>>>(C, g, V, c);
+    col_partial_kernel<true><<<dim3(g.ncb, g.nrb), 256, 0, st>>>(C, g, V, c);
     WOTG_LAUNCHED();
-    col_combine_kernel<true><<<vec_blocks(g.J), 256, 0, st>>>(g, V, c, parity);
+    col_combine_kernel<true, true><<<vec_blocks(g.J), 256, 0, st>>>(g, V, c, parity);
     WOTG_LAUNCHED();
     return WOTG_OK;
   }
@@ -780,7 +834,7 @@ struct Solver {
 
   int fresh_lrow(const Coef& c) {
     if (tc.on) return tc_row_pass<false>(c, 0);
-    row_pass_kernel<false><<<g.row_grid, 256, 0, st>>>(C, g, V, c, 0);
+    row_pass_kernel<false, true><<<g.row_grid, 256, 0, st>>>(C, g, V, c, 0);
     WOTG_LAUNCHED();
     return WOTG_OK;
   }
@@ -960,8 +1014,8 @@ static Geom make_geom(int64_t I, int64_t J, int64_t ldc) {
   g.J = J;
   g.ldc = ldc;
   const int sms = sm_count();
-  static const int occ_row = occupancy(row_pass_kernel<true>);
-  static const int occ_col = occupancy(col_partial_kernel);
+  static const int occ_row = occupancy(row_pass_kernel<true, true>);
+  static const int occ_col = occupancy(col_partial_kernel<true>);
   const int64_t max_warps = (int64_t)sms * occ_row * 8;
   const int64_t rows_per_warp = (I + max_warps - 1) / max_warps;
   const int64_t warps = (I + rows_per_warp - 1) / rows_per_warp;
@@ -990,6 +1044,8 @@ static size_t layout(Bump& b, const Geom& g, Vecs& V) {
   V.Lcol = b.take<double>(g.J);
   V.wrow = b.take<float>(g.I);
   V.wcol = b.take<float>(g.ldc);
+  V.wrow_lo = b.take<float>(g.I);
+  V.wcol_lo = b.take<float>(g.ldc);
   V.part = b.take<float2>((size_t)g.nrb * g.ldc);
   V.maxslot = b.take<unsigned long long>(2);
   V.red = b.take<double>((size_t)kRedBlocks * kNq);
@@ -1022,7 +1078,7 @@ extern "C" int wotg_lse_matvec(const float* C, int64_t I, int64_t J, int64_t ldc
   if (axis == 0) {
     V.wcol = const_cast<float*>(w);
     V.Lrow = L;
-    row_pass_kernel<false><<<g.row_grid, 256, 0, st>>>(C, g, V, c, 0);
+    row_pass_kernel<false, false><<<g.row_grid, 256, 0, st>>>(C, g, V, c, 0);
     WOTG_LAUNCHED();
     return WOTG_OK;
   }
@@ -1030,9 +1086,9 @@ extern "C" int wotg_lse_matvec(const float* C, int64_t I, int64_t J, int64_t ldc
   V.wrow = const_cast<float*>(w);
   V.Lcol = L;
   V.part = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
-  col_partial_kernel<<<dim3(g.ncb, g.nrb), 256, 0, st>>>(C, g, V, c);
+  col_partial_kernel<false><<<dim3(g.ncb, g.nrb), 256, 0, st>>>(C, g, V, c);
   WOTG_LAUNCHED();
-  col_combine_kernel<false><<<(unsigned)((J + 255) / 256), 256, 0, st>>>(g, V, c, 0);
+  col_combine_kernel<false, false><<<(unsigned)((J + 255) / 256), 256, 0, st>>>(g, V, c, 0);
   WOTG_LAUNCHED();
   return WOTG_OK;
 }

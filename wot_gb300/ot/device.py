@@ -138,12 +138,25 @@ FORMS = {'materialized': N.FORM_MATERIALIZED, 'onthefly': N.FORM_ONTHEFLY}
 TC_MAX_DIM = 62   # point dimensions the tensor-core half-step packs (two bias columns in 64)
 
 
+# Below this many cost entries the two forms take about the same time (measured
+# on GB300 at 30 dimensions: 1500 x 1800 cells 24 ms streamed against 30 ms on
+# the tensor cores per solve, 2500 x 3000 32 ms against 30 ms, 9000 x 10800
+# 93 ms against 43 ms), so 'auto' keeps the streamed form there: its exponents
+# are exact to the FP32 storage of C, while the tensor-core form's carry the
+# error of the points' 22-bit FP16 hi/lo split accumulated in FP32 (about
+# kappa |x| |y| 2^-22 per exponent).
+TC_AUTO_MIN_ENTRIES = 4_000_000
+
+
 def resolve_form(cost: DeviceCost, form: str) -> int:
     """'materialized' streams the FP32 cost; 'onthefly' recomputes cost tiles
     from the points on the tensor cores; 'auto' picks the latter when the cost
-    was built from points of at most TC_MAX_DIM dimensions."""
+    was built from points of at most TC_MAX_DIM dimensions and has at least
+    TC_AUTO_MIN_ENTRIES entries (where it is the faster form)."""
     if form == 'auto':
-        form = 'onthefly' if cost.X is not None and cost.X.shape[1] <= TC_MAX_DIM else 'materialized'
+        tc = (cost.X is not None and cost.X.shape[1] <= TC_MAX_DIM
+              and cost.I * cost.J >= TC_AUTO_MIN_ENTRIES)
+        form = 'onthefly' if tc else 'materialized'
     if form not in FORMS:
         raise ValueError("form must be 'auto', 'materialized' or 'onthefly'")
     if form == 'onthefly' and cost.X is None:
