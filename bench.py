@@ -225,16 +225,88 @@ COURSE_CFG = dict(growth_iters=1, lambda2=50, epsilon0=1, tau=10000, scaling_ite
                   tolerance=1e-8, max_iter=1e7, batch_size=5, extra_iter=1000)
 
 
-def course_days(n_days, seed=0):
+def course_items(n_days):
+    """The course's day sizes, pair shapes and items (pair, parameters): every
+    consecutive pair x the epsilon x lambda1 grid."""
+    from wot_gb300 import synthetic
+    sizes = synthetic.log_uniform_day_sizes(n_days, 1000, 30000, seed=2)
+    shapes = [(int(sizes[t]), int(sizes[t + 1])) for t in range(n_days - 1)]
+    items = [(p, dict(COURSE_CFG, epsilon=e, lambda1=l)) for p in range(n_days - 1) for e in COURSE_EPS
+             for l in COURSE_L1]
+    return sizes, shapes, items
+
+
+def course_days(n_days, seed=0, needed=None):
     """Per-day cells of the long synthetic time course (day sizes log-uniform in
-    [1000, 30000]), generated in a spawn process pool before any CUDA call."""
+    [1000, 30000]), generated in a spawn process pool before any CUDA call;
+    with ``needed`` (day indices), only those days (the others are None)."""
     import multiprocessing as mp
     from wot_gb300 import synthetic
     sizes = synthetic.log_uniform_day_sizes(n_days, 1000, 30000, seed=2)
     prof = synthetic.course_profiles(n_days, GENES, CLUSTERS, seed)
-    with mp.get_context('spawn').Pool(min(16, os.cpu_count() or 1)) as pool:
-        days = pool.starmap(synthetic.course_day, [(prof, t, int(n)) for t, n in enumerate(sizes)])
+    want = sorted(set(range(n_days)) if needed is None else set(needed))
+    with mp.get_context('spawn').Pool(max(1, min(16, os.cpu_count() or 1, len(want)))) as pool:
+        made = pool.starmap(synthetic.course_day, [(prof, t, int(sizes[t])) for t in want])
+    days = [None] * n_days
+    for t, d in zip(want, made):
+        days[t] = d
     return sizes, days
+
+
+def run_course_sharded(args, days_data, rank, world, pg):
+    """The course under torchrun: the items split over the ranks by estimated
+    work (wot_gb300.ot.shard), each rank building the costs of only its own
+    pairs and solving its items in one wotg_solve_batched call per step; the
+    job's time is the slowest rank's. Strong scaling: the whole course (1000
+    maps) is the work at every rank count."""
+    import torch
+    from wot_gb300 import _build, _native
+    from wot_gb300.ot import batch as Bt, device as D, shard
+    from wot_gb300.ot.util import compute_pca
+    import logging
+    logging.disable(logging.WARNING)
+    _build.build()
+    lib = _native.load()
+    sizes, days = days_data
+    _, shapes, items = course_items(len(days))
+    mine = shard.my_items(shapes, items, rank, world)
+    used = sorted({items[k][0] for k in mine})
+    local = {p: i for i, p in enumerate(used)}
+    pairs = []
+    for t in used:
+        x0, x1, sv, _ = compute_pca(days[t][0], days[t + 1][0], PCA_D)
+        cost = D.default_cost((x0 * sv).float().contiguous(), (x1 * sv).float().contiguous())
+        pairs.append(Bt.prepare_pair(cost, days[t][1]))
+    my = [(local[items[k][0]], items[k][1]) for k in mine]
+    for _ in range(args.warmup):
+        maps = Bt.solve_batched(pairs, my)
+    torch.cuda.synchronize()
+    pg.barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    n_launch0 = lib.wotg_launch_count()
+    with Clocks(dist_env()[2]) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            maps = Bt.solve_batched(pairs, my)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    t = shard.max_over_ranks(ev0.elapsed_time(ev1) / 1e3 / args.steps)
+    its = shard.gather([(k, int(m.stats['iterations'])) for k, m in zip(mine, maps)])
+    if rank != 0:
+        return None
+    return {'metric': METRIC, 'value': len(items) / t, 'unit': 'maps/s', 'n_gpus': world, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': t * 1e3, 'higher_is_better': True, 'scaling': 'strong',
+            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': 'batched time course: %d days (log-uniform 1000-30000 cells), %d pairs x eps %s '
+                                   'x lambda1 %s, items split over %d ranks by estimated work'
+                                   % (len(days), len(shapes), list(COURSE_EPS), list(COURSE_L1), world),
+                       'pairs': len(shapes), 'items': len(items), 'parallelism': 'item shards x %d' % world,
+                       'timed': 'each rank: one wotg_solve_batched call over its items, costs resident; '
+                                'max over ranks'},
+            'sinkhorn_iter_per_s': float(sum(i for _, i in its)) / t,
+            'gpu_launches': int(lib.wotg_launch_count() - n_launch0), 'clocks': clk.summary(), 'e2e': None}
 
 
 def run_course(args, days_data):
@@ -259,7 +331,7 @@ def run_course(args, days_data):
         cost = D.default_cost(a, b)
         pairs.append(Bt.prepare_pair(cost, days[t][1]))   # G = growth ** (t1 - t0), t1 - t0 = 1
         pts.append((a, b))
-    items = [(p, dict(COURSE_CFG, epsilon=e, lambda1=l)) for p in range(npairs) for e in COURSE_EPS for l in COURSE_L1]
+    _, _, items = course_items(len(days))
     stream = torch.cuda.current_stream()
     for _ in range(args.warmup):
         maps = Bt.solve_batched(pairs, items)
@@ -564,9 +636,25 @@ def main():
         print(json.dumps(run_adjoint(args)), flush=True)
         return
     if args.workload == 'course' and args.impl != 'reference':
+        rank, world, local = dist_env()
+        if world > 1:
+            from wot_gb300.ot import shard
+            _, shapes, items = course_items(args.course_days)
+            mine = shard.my_items(shapes, items, rank, world)
+            need = {items[k][0] for k in mine} | {items[k][0] + 1 for k in mine}
+            data = course_days(args.course_days, needed=need)
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(local)
+            dist.init_process_group('nccl')
+            line = run_course_sharded(args, data, rank, world, dist)
+            if line is not None:
+                print(json.dumps(line), flush=True)
+            dist.destroy_process_group()
+            return
         data = course_days(args.course_days)
         import torch
-        torch.cuda.set_device(dist_env()[2])
+        torch.cuda.set_device(local)
         print(json.dumps(run_course(args, data)), flush=True)
         return
     if args.pair:

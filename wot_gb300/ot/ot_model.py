@@ -197,7 +197,7 @@ class OTModel:
         if learned_tables:
             write_learned_growth(learned_tables, os.path.join(tmap_dir, tmap_prefix + '_g.txt'))
 
-    def compute_transport_maps_batched(self, day_pairs=None, sweep=None):
+    def compute_transport_maps_batched(self, day_pairs=None, sweep=None, rank=0, world=1, group=None):
         """Every day pair (the consecutive days, or ``day_pairs``) for every
         parameter set of ``sweep`` (a list of ot_config overrides, e.g.
         ``[{'epsilon': e, 'lambda1': l} for e in ... for l in ...]``; default:
@@ -209,38 +209,57 @@ class OTModel:
         the solver is the duality-gap one. Returns a dict
         {(t0, t1, i): ImplicitMap} with i the index into ``sweep``; an
         ImplicitMap holds the map as potentials (``.dense()``, ``.pull_back``,
-        ``.push_forward``, ``.row_sums``, ``.stats``)."""
+        ``.push_forward``, ``.row_sums``, ``.stats``).
+
+        With ``world`` > 1 (one process per GPU, ``torch.distributed``
+        initialised, ``rank`` this process's rank) the items are split over the
+        ranks by estimated work (``shard.solve_sharded``): each rank builds the
+        costs of only the pairs its items use and returns only the maps it
+        solved. ``self.batch_summary`` then lists every item's key, status,
+        iteration count and the rank that holds its map, on every rank."""
         from . import batch as B
+        from . import shard as S
         if self.solver is not ot.optimal_transport_duality_gap:
             raise ValueError('batched solves use the duality-gap solver')
         t = self.timepoints
         pairs_days = list(day_pairs) if day_pairs else [(t[i], t[i + 1]) for i in range(len(t) - 1)]
         sweep = list(sweep) if sweep else [{}]
-        pairs, keys = [], []
+        keys, selections = [], []
         for t0, t1 in pairs_days:
             config = {**self.ot_config, 't0': t0, 't1': t1, 'covariate': None}
             p0, p1 = self.select_pair(config)
             if p0.shape[0] == 0 or p1.shape[0] == 0:
                 continue
-            local_pca = config.get('local_pca')
+            keys.append((t0, t1))
+            selections.append((p0, p1))
+
+        def build_pair(p):
+            (t0, t1), (p0, p1) = keys[p], selections[p]
+            local_pca = self.ot_config.get('local_pca')
             if local_pca is not None and local_pca > 0:
                 x0, x1, sv, _ = compute_pca(p0.X, p1.X, local_pca, solver=self.pca)
                 cost = OTModel.compute_default_cost_matrix(x0, x1, sv)
             else:
                 cost = OTModel.compute_default_cost_matrix(p0.X, p1.X)
-            delta = t1 - t0
             if self.cell_growth_rate_field in ds_.columns(p0.obs):
-                G = np.power(ds_.column(p0.obs, self.cell_growth_rate_field).astype(np.float64), delta)
+                G = np.power(ds_.column(p0.obs, self.cell_growth_rate_field).astype(np.float64), t1 - t0)
             else:
                 G = np.ones(p0.shape[0])
-            pairs.append(B.prepare_pair(cost, G))
-            keys.append((t0, t1))
+            return B.prepare_pair(cost, G)
+
         items, names = [], []
         for p, (t0, t1) in enumerate(keys):
             for i, over in enumerate(sweep):
                 items.append((p, {**self.ot_config, **over}))
                 names.append((t0, t1, i))
-        maps = B.solve_batched(pairs, items)
+        if world > 1:
+            shapes = [(p0.shape[0], p1.shape[0]) for p0, p1 in selections]
+            maps, summary = S.solve_sharded(shapes, items, build_pair, rank, world, group)
+            self.batch_summary = [(names[k], rec) for k, rec in summary]
+            return {names[k]: m for k, m in maps.items()}
+        maps = B.solve_batched([build_pair(p) for p in range(len(keys))], items)
+        self.batch_summary = [(names[k], {'rank': 0, 'status': m.status, 'stats': m.stats})
+                              for k, m in enumerate(maps)]
         return dict(zip(names, maps))
 
     def compute_transport_map(self, t0, t1, covariate=None, cost_matrix=None):
