@@ -47,6 +47,7 @@ def parse():
     ap.add_argument('--pair', default=None, help='I,J cells of a smaller pair (profiling runs)')
     ap.add_argument('--pca', type=int, default=None, help='local PCA dimension of the pair workload (profiling runs)')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-parity', action='store_true', help='skip the full-size FP64 parity checks')
     ap.add_argument('--workload', default='pair', choices=['pair', 'course', 'chain', 'adjoint'],
                     help="pair: one 20000x25000 map per step; course: the batched 41-day time course x "
                          "5x5 epsilon/lambda1 sweep (1000 maps) per step; chain: the 60000x60000 map and "
@@ -174,6 +175,46 @@ def cpu_sample(a, b, G, I_s, J_s, rng, stages=None):
     return time.perf_counter() - t0, iters[0], T, (a_s, b_s, G_s)
 
 
+def dev_errors(T, R):
+    """Parity of a device coupling T with the FP64 reference R (torch tensors):
+    max|T - R| / max|R|; max |T - R| / |R| over the entries |R| >= 1e-6 max|R|;
+    the row and column marginals' max |r - r_ref| / max r_ref."""
+    import torch
+    T = T.to(torch.float64)
+    mx = R.abs().max()
+    d = (T - R).abs()
+    ce = float(d.max() / mx)
+    keep = R.abs() >= 1e-6 * mx
+    ee = float((d[keep] / R.abs()[keep]).max())
+    del d, keep
+    rr, rc = R.sum(1), R.sum(0)
+    me = max(float((T.sum(1) - rr).abs().max() / rr.abs().max()), float((T.sum(0) - rc).abs().max() / rc.abs().max()))
+    return {'coupling_max_rel_err': ce, 'element_max_rel_err': ee, 'marginal_max_rel_err': me}
+
+
+def fp64_reference(a, b, G, cfg):
+    """The reference's solver in FP64 on the GPU (oracle/torch_ot.py, the same
+    arithmetic as the NumPy oracle) on the cost of the FP32 coordinates a, b:
+    returns (coupling, iterations, seconds)."""
+    import torch
+    from oracle import torch_ot as tot
+    t0 = time.perf_counter()
+    C64 = tot.default_cost(a.double(), b.double())
+    its = [0]
+
+    def counting(**kw):
+        st = {}
+        out = tot.optimal_transport_duality_gap(stats=st, **kw)
+        its[0] += st['iterations']
+        return out
+
+    R, _ = tot.compute_transport_matrix(solver=counting, C=C64, G=torch.as_tensor(G, device='cuda').double(),
+                                        **dict(cfg))
+    del C64
+    torch.cuda.synchronize()
+    return R, its[0], time.perf_counter() - t0
+
+
 def blas_threads():
     for k in ('OPENBLAS_NUM_THREADS', 'OMP_NUM_THREADS', 'MKL_NUM_THREADS'):
         if os.environ.get(k):
@@ -203,12 +244,15 @@ def run_reference(args):
     t_step = float(np.mean(times))
     it_s = float(np.mean(its))
     scale = (I_FULL * J_FULL) / (I_s * J_s)
-    # maps/s at full size assuming the same iteration count as the sample
+    # maps/s at full size from the sample's time scaled by I*J (the whole-pair oracle solve on the
+    # GPU host's cores took 0.9-1.1x of this extrapolation: profiles/cpu_oracle_fullsize_20000x25000.md)
     value = 1.0 / (t_step * scale)
     sample = ('%dx%d random cell subsample of the 20000x25000 pair per step (own median), full FP64 oracle '
-              'duality-gap solve x3 growth iterations (%.0f iterations); maps/s extrapolated by I*J' % (I_s, J_s, it_s))
+              'duality-gap solve x3 growth iterations (%.0f iterations); ms_per_step is the measured time of '
+              'one such step, value its maps/s extrapolated to the whole pair by I*J' % (I_s, J_s, it_s))
     line = {'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': 'maps/s', 'n_gpus': args.gpus,
-            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': t_step * scale * 1e3,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': t_step * 1e3,
+            'ms_per_map_extrapolated': t_step * scale * 1e3,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
             'config': {'workload': WORKLOAD, 'I': I_FULL, 'J': J_FULL, 'd': PCA_D},
             'sinkhorn_iter_per_s': it_s / t_step * (I_s * J_s) / (I_FULL * J_FULL),
@@ -376,6 +420,27 @@ def run_course(args, days_data):
     best_plain = min(t_plain.values())
 
     hbm_peak, tf_peak, peak_kind = peaks()
+    # the dominant kernel: one batched pass over every item of every pair, as the solve's autotuner
+    # timed it with CUDA events for the configuration it chose (row direction: rows of C)
+    import ctypes
+    ms_r, ms_c = ctypes.c_float(0.0), ctypes.c_float(0.0)
+    kgrw = (ctypes.c_int32 * 4)()
+    _native.check(lib.wotg_batch_pass_timing(ctypes.byref(ms_r), ctypes.byref(ms_c), kgrw), 'wotg_batch_pass_timing')
+    elems = float(sum(pairs[p].cost.I * pairs[p].cost.J for p, _ in items))
+    pass_bytes = float(sum(4 * p.cost.I * p.cost.J for p in pairs))
+    exp_pk = exp2_peak()
+    t_pass = ms_r.value * 1e-3
+    roofline = {'bound': 'hbm', 'achieved': pass_bytes / t_pass / 1e9, 'peak': hbm_peak, 'unit': 'GB/s',
+                'frac': pass_bytes / t_pass / 1e9 / hbm_peak, 'traffic': None,
+                'kernel': 'pass_kernel<%d,%d,speculative> (rows of C)' % (kgrw[0], kgrw[1]), 'peak_kind': peak_kind,
+                'launch_ms': ms_r.value, 'col_launch_ms': ms_c.value,
+                'col_kernel': 'pass_kernel<%d,%d,speculative> (rows of CT)' % (kgrw[2], kgrw[3]),
+                'element_evaluations_per_launch': elems,
+                'element_evaluations_per_s': elems / t_pass, 'exp2_peak_per_s': exp_pk,
+                'exp2_frac': (elems / t_pass / exp_pk) if exp_pk else None,
+                'note': 'one launch evaluates every item of every pair against the pair\'s cost, read once for '
+                        'all its items (the algorithmic bytes); the bound is the one exp2 per element '
+                        'evaluation (exp2_frac), not HBM'}
     line = {'metric': METRIC, 'value': len(items) / t, 'unit': 'maps/s', 'n_gpus': 1, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': t * 1e3, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
@@ -401,7 +466,8 @@ def run_course(args, days_data):
                 'note': 'plain = wotg_compute_transport_matrix per item (potentials out), the faster of the '
                         'on-the-fly and materialised forms; full-course plain time extrapolated from the subset '
                         'by sum(iterations * I * J)'},
-            'gpu_launches': int(launches), 'clocks': clk.summary(), 'peaks': {'kind': peak_kind}}
+            'gpu_launches': int(launches), 'clocks': clk.summary(), 'peaks': {'kind': peak_kind},
+            'roofline': roofline}
     if not args.no_cpu:
         # parity and CPU baseline: the oracle on items of the smallest pair
         from oracle import ot_model as oom, optimal_transport as oot
@@ -429,8 +495,69 @@ def run_course(args, days_data):
                                 'sample': 'oracle FP64 solves of %d items of the smallest pair (%dx%d, %.1f s); '
                                           'extrapolated to all items by sum(iterations * I * J)'
                                           % (len(checks), C.shape[0], C.shape[1], t_cpu)}
-    line['e2e'] = None
+    if not getattr(args, 'no_parity', False):
+        # FP64 reference parity (the reference's solver restated in FP64 on the GPU): every pair at
+        # eps 0.05 / lambda1 1, and the whole eps x lambda1 grid on the three smallest pairs
+        smallest = [int(p) for p in order[:3]]
+        checks = [(p, 0.05, 1) for p in range(npairs)]
+        checks += [(p, e, l) for p in smallest for e in COURSE_EPS for l in COURSE_L1 if (e, l) != (0.05, 1)]
+        recs = []
+        t0 = time.perf_counter()
+        for p, e, l in checks:
+            cfg = dict(COURSE_CFG, epsilon=e, lambda1=l)
+            k = items.index((p, cfg))
+            R, it_ref, _ = fp64_reference(pts[p][0], pts[p][1], days[p][1], cfg)
+            T = maps[k].dense()
+            r = dev_errors(T, R)
+            del R, T
+            r.update(pair=p, shape=[int(pairs[p].cost.I), int(pairs[p].cost.J)], eps=e, lambda1=l,
+                     iterations_gpu=int(maps[k].stats['iterations']), iterations_oracle=int(it_ref))
+            recs.append(r)
+        torch.cuda.empty_cache()
+        keys = ('coupling_max_rel_err', 'element_max_rel_err', 'marginal_max_rel_err')
+        line['parity_full'] = {
+            'oracle': 'the reference solver restated in FP64 on the GPU (oracle/torch_ot.py), same coordinates',
+            'items': len(recs), 'pairs_at_eps0.05_lambda1_1': npairs, 'full_grid_pairs': smallest,
+            'max': {k: max(r[k] for r in recs) for k in keys},
+            'iterations_equal': sum(r['iterations_gpu'] == r['iterations_oracle'] for r in recs),
+            'iterations_max_abs_diff': max(abs(r['iterations_gpu'] - r['iterations_oracle']) for r in recs),
+            'worst_marginal': sorted(recs, key=lambda r: -r['marginal_max_rel_err'])[:3],
+            'seconds': time.perf_counter() - t0}
+    line['e2e'] = course_e2e(days, sizes) if not getattr(args, 'no_e2e', False) else None
     return line
+
+
+def course_e2e(days, sizes):
+    """The course through the public API on host data: a Dataset of every day's
+    expression (host FP32), OTModel(...).compute_transport_maps_batched over
+    the consecutive pairs x the 5 x 5 sweep (device PCA, cost and median per
+    pair, the batched solve), then every map's potentials read back to the
+    host. One timed call after one untimed call."""
+    import torch
+    import wot_gb300 as wot
+    X = np.vstack([d[0] for d in days])
+    day = np.concatenate([np.full(len(d[0]), float(t)) for t, d in enumerate(days)])
+    growth = np.concatenate([d[1] for d in days])
+    ds = wot.Dataset(X, wot.Frame({'day': day, 'cell_growth_rate': growth}, index=np.arange(len(day)).astype(str)))
+    sweep = [{'epsilon': e, 'lambda1': l} for e in COURSE_EPS for l in COURSE_L1]
+    model = wot.OTModel(ds, growth_iters=1, local_pca=PCA_D)
+
+    def call():
+        maps = model.compute_transport_maps_batched(sweep=sweep)
+        host = {k: (m.u_bar.cpu().numpy(), m.v_bar.cpu().numpy()) for k, m in maps.items()}
+        return maps, host
+
+    call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    maps, host = call()
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    d2h = int(sum(u.nbytes + v.nbytes for u, v in host.values()))
+    return {'value': len(maps) / t, 'unit': 'maps/s', 'seconds': t,
+            'h2d_bytes_per_step': int(X.nbytes + growth.nbytes), 'd2h_bytes_per_step': d2h,
+            'api': 'wot_gb300.OTModel(Dataset of %d days).compute_transport_maps_batched(sweep of 25) '
+                   '(device PCA + cost per pair + batched solve; potentials to host)' % len(days)}
 
 
 CHAIN_CFG = dict(growth_iters=1, epsilon=0.05, lambda1=1, lambda2=50, epsilon0=1, tau=10000, scaling_iter=3000,
@@ -857,6 +984,21 @@ def main():
                                           'iterations (%.1f s, %d iterations); extrapolated to 20000x25000 by '
                                           'I*J*iterations' % (SAMPLE[0], SAMPLE[1], t_cpu, it_cpu),
                                 'sample_stages_s': {k: round(v, 3) for k, v in stages.items()}}
+    if rank == 0 and not args.no_parity:
+        # the whole pair against the reference's solver in FP64 (same coordinates, all growth iterations)
+        G_dev = growth[day == 0]
+        R, it_ref, t_ref = fp64_reference(a, b, G_dev, CFG)
+        full = {'shape': [I_FULL, J_FULL], 'oracle': 'the reference solver restated in FP64 on the GPU '
+                                                     '(oracle/torch_ot.py, equal to the NumPy oracle)',
+                'iterations_oracle': it_ref, 'oracle_s': t_ref}
+        full[line['form']] = dict(dev_errors(tmap, R), iterations_gpu=int(iters / args.steps))
+        other = 'materialized' if line['form'] == 'onthefly' else 'onthefly'
+        res_o = D.solve(D.default_cost(a, b), G, CFG, _native.SOLVER_DUALITY_GAP, want_tmap=True, tmap_out=tmap,
+                        form=other)
+        full[other] = dict(dev_errors(tmap, R), iterations_gpu=int(res_o.stats['iterations']))
+        line['parity_full'] = full
+        del R
+        torch.cuda.empty_cache()
 
     if extra:
         # the batched time course (one warm-up, one timed batch), the large-pair chain and the gradient
@@ -874,9 +1016,27 @@ def main():
                 line[key] = {'error': repr(e)}
             torch.cuda.empty_cache()
     if rank == 0:
+        print('summary: ' + json.dumps(summary_of(line)), file=sys.stderr, flush=True)
         print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()
+
+
+def summary_of(line):
+    """The headline figures of the JSON line (printed to stderr beside it)."""
+    out = {'pair_maps_per_s': line.get('value'), 'pair_e2e': (line.get('e2e') or {}).get('value'),
+           'pair_parity_full': {k: v for k, v in (line.get('parity_full') or {}).items()
+                                if k in ('onthefly', 'materialized')}}
+    c = line.get('course') or {}
+    if 'value' in c:
+        out['course'] = {'maps_per_s': c['value'], 'e2e': (c.get('e2e') or {}).get('value'),
+                         'ratio_vs_best_plain': c['batched_vs_plain']['ratio_vs_best_plain'],
+                         'exp2_frac': (c.get('roofline') or {}).get('exp2_frac'),
+                         'parity_max': (c.get('parity_full') or {}).get('max')}
+    for k in ('chain', 'adjoint'):
+        if 'value' in (line.get(k) or {}):
+            out[k] = line[k]['value']
+    return out
 
 
 if __name__ == '__main__':

@@ -295,6 +295,16 @@ int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const wotg_item*
                        double* u_bar, double* v_bar, double* row_sums, double* learned_growth, wotg_stats* stats,
                        int32_t* statuses, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Diagnostic (no counterpart in the reference): the device time of one batched
+ * pass over every item of every pair (speculative form, zero weights, no
+ * epilogue: the exp-bound core of each half-step) for the configuration the
+ * autotuner of the last wotg_solve_batched call in this process chose, as it
+ * measured it with CUDA events (best of two launches), per direction: ms_row
+ * over the rows of C, ms_col over the rows of CT; kg_rw (4 ints, may be NULL)
+ * receives (items per register group, rows per warp) of each. WOTG_BADARG
+ * before any batched solve. Host-side, no device work. */
+int wotg_batch_pass_timing(float* ms_row, float* ms_col, int32_t* kg_rw);
+
 /* Multi right-hand-side half-step on one materialised cost (row form of
  * wotg_lse_matvec for K weight vectors at once; each cost element is read once):
  *   L[k * ldl + i] = ln2 * log2 sum_j 2^(W[k * ldw + j] - kappa2[k] C_ij),  k < K

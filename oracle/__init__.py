@@ -10,6 +10,9 @@ the unbalanced entropic OT transport-map path (wot 1.0.8):
   squared-Euclidean cost, per-pair orchestration) and ``wot/ot/util.py``
   ``compute_pca`` (restated with an exact SVD; the reference uses
   scikit-learn's randomized SVD, see that module);
+* ``oracle.torch_ot``          — the default solver and the cost again, on FP64
+  torch tensors in the same operation order, so that the same reference
+  arithmetic checks 20,000 x 25,000 and larger problems on a GPU;
 * ``oracle.tmap``              — ``wot/tmap/transport_map_model.py``,
   ``wot/tmap/chaining.py``, ``wot/tmap/util.py`` and ``wot/population.py``.
 

@@ -136,3 +136,31 @@ def test_adjoint_reference_fixed_point_and_gradient():
     ad = [float({'x': gx, 'y': gy, 'logg': gl}[n][i]) for n, i in coords]
     gmax = max(float(gx.abs().max()), float(gy.abs().max()), float(gl.abs().max()))
     assert max(abs(a - f) for a, f in zip(ad, fd)) <= 1e-6 * gmax
+
+
+def test_torch_fp64_restatement_matches_numpy_oracle(pair_golden):
+    """oracle.torch_ot (the same FP64 reference arithmetic on torch tensors, the
+    checker for full-size problems on the GPU) equals the NumPy oracle, which is
+    pinned to the reference's golden outputs: couplings, iteration and
+    absorption counts, growth iterations, the median-normalised cost."""
+    import ast
+    import torch
+    from oracle import ot_model as oom, optimal_transport as oot, torch_ot as tot
+    z = pair_golden
+    defaults = dict(growth_iters=1, epsilon=0.05, lambda1=1, lambda2=50, epsilon0=1, tau=10000, tolerance=1e-8,
+                    max_iter=1e7, batch_size=5)
+    for name in ('dg_default', 'dg_growth3', 'dg_eps01_lam10', 'dg_tau10', 'dg_maxiter'):
+        cfg = dict(defaults, **ast.literal_eval(str(z['params_' + name])))
+        st_n, st_t = {}, {}
+        ref, lg_n = oot.compute_transport_matrix(solver=lambda **k: oot.optimal_transport_duality_gap(stats=st_n, **k),
+                                                 C=z['C'], G=z['G'].copy(), **cfg)
+        got, lg_t = tot.compute_transport_matrix(solver=lambda **k: tot.optimal_transport_duality_gap(stats=st_t, **k),
+                                                 C=torch.as_tensor(z['C']), G=torch.as_tensor(z['G']), **cfg)
+        assert np.abs(got.numpy() - ref).max() <= 1e-10 * np.abs(ref).max(), name
+        assert st_t['iterations'] == st_n['iterations'] and st_t['absorptions'] == st_n['absorptions'], name
+        assert np.allclose(np.array([x.numpy() for x in lg_t]), np.array(lg_n), rtol=1e-10, atol=0)
+    rng = np.random.default_rng(2)
+    a, b = rng.normal(size=(41, 7)), rng.normal(size=(58, 7))
+    for (x, y) in ((a, b), (a[:40], b)):   # odd and even entry counts of the median
+        np.testing.assert_allclose(tot.default_cost(torch.as_tensor(x), torch.as_tensor(y)).numpy(),
+                                   oom.compute_default_cost_matrix(x, y), rtol=1e-13, atol=1e-13)

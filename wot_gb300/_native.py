@@ -38,6 +38,7 @@ EXPORTS = (
     'wotg_solve_batched', 'wotg_lse_matvec_multi_workspace_bytes', 'wotg_lse_matvec_multi',
     'wotg_coupling_from_potentials', 'wotg_ot_adjoint_workspace_bytes', 'wotg_ot_adjoint',
     'wotg_refine_potentials', 'wotg_exp2_rate', 'wotg_lse_points_timing', 'wotg_lse_points_bounded',
+    'wotg_batch_pass_timing',
 )
 
 
@@ -106,6 +107,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         'wotg_tc_selftest': (ctypes.c_int, [vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, i32, vp, vp]),
         'wotg_lse_points_workspace_bytes': (ctypes.c_size_t, [i64, i64, i32]),
         'wotg_lse_points': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, vp, vp, vp, ctypes.c_size_t, vp]),
+        'wotg_batch_pass_timing': (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                                  ctypes.POINTER(ctypes.c_int32)]),
         'wotg_lse_points_bounded': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, vp, vp, ctypes.c_uint32,
                                                    vp, ctypes.c_size_t, vp]),
         'wotg_compute_transport_matrix': (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params),

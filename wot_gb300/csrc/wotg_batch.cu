@@ -1188,8 +1188,14 @@ struct TuneKey {
     return std::tie(dir, np, ni, work) < std::tie(o.dir, o.np, o.ni, o.work);
   }
 };
-static std::map<TuneKey, int> g_tuned;
+struct Tuned {
+  int cfg;
+  float ms;   // measured time of one pass of that configuration
+};
+static std::map<TuneKey, Tuned> g_tuned;
 static std::mutex g_tune_mu;
+// The last batch's choice and measured pass time per direction (wotg_batch_pass_timing).
+static Tuned g_last_tuned[2] = {{-1, 0.f}, {-1, 0.f}};
 
 static int autotune(const Layout& L, const int* chk_off, int dir, int np, int ni, long long work,
                     const std::vector<Entry>& probe, const std::vector<int>& probe_n, cudaStream_t st,
@@ -1199,7 +1205,8 @@ static int autotune(const Layout& L, const int* chk_off, int dir, int np, int ni
     std::lock_guard<std::mutex> g(g_tune_mu);
     auto f = g_tuned.find(key);
     if (f != g_tuned.end()) {
-      *choice = f->second;
+      *choice = f->second.cfg;
+      g_last_tuned[dir] = f->second;
       return WOTG_OK;
     }
   }
@@ -1244,7 +1251,8 @@ static int autotune(const Layout& L, const int* chk_off, int dir, int np, int ni
   if (status) return status;
   *choice = best_i;
   std::lock_guard<std::mutex> g(g_tune_mu);
-  g_tuned[key] = best_i;
+  g_tuned[key] = Tuned{best_i, best};
+  g_last_tuned[dir] = Tuned{best_i, best};
   return WOTG_OK;
 }
 
@@ -1581,5 +1589,20 @@ extern "C" int wotg_lse_matvec_multi(const float* C, int64_t I, int64_t J, int64
   cfg.exact<<<pass_grid(cfg.exact), kThreads, 0, st>>>(A);
   WOTG_LAUNCHED();
   // the host tables above are pageable: the copies finished before this returns
+  return WOTG_OK;
+}
+
+extern "C" int wotg_batch_pass_timing(float* ms_row, float* ms_col, int32_t* kg_rw) {
+  using namespace wotg::batch;
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  if (g_last_tuned[0].cfg < 0 || g_last_tuned[1].cfg < 0) return WOTG_BADARG;
+  if (ms_row) *ms_row = g_last_tuned[0].ms;
+  if (ms_col) *ms_col = g_last_tuned[1].ms;
+  if (kg_rw) {
+    kg_rw[0] = kCfgs[g_last_tuned[0].cfg].kg;
+    kg_rw[1] = kCfgs[g_last_tuned[0].cfg].rw;
+    kg_rw[2] = kCfgs[g_last_tuned[1].cfg].kg;
+    kg_rw[3] = kCfgs[g_last_tuned[1].cfg].rw;
+  }
   return WOTG_OK;
 }
