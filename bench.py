@@ -390,6 +390,12 @@ def run_course(args, days_data):
         torch.cuda.synchronize()
     launches = lib.wotg_launch_count() - n_launch0
     t = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    # the dominant kernel: one batched pass over every item of every pair, as this batch's autotuner
+    # timed it with CUDA events for the configuration it chose (row direction: rows of C)
+    import ctypes
+    ms_r, ms_c = ctypes.c_float(0.0), ctypes.c_float(0.0)
+    kgrw = (ctypes.c_int32 * 4)()
+    _native.check(lib.wotg_batch_pass_timing(ctypes.byref(ms_r), ctypes.byref(ms_c), kgrw), 'wotg_batch_pass_timing')
     its = np.array([m.stats['iterations'] for m in maps], dtype=np.float64)
     ij = np.array([m.shape[0] * m.shape[1] for m in maps], dtype=np.float64)
     work = float(np.sum(its * ij * 2))
@@ -420,12 +426,6 @@ def run_course(args, days_data):
     best_plain = min(t_plain.values())
 
     hbm_peak, tf_peak, peak_kind = peaks()
-    # the dominant kernel: one batched pass over every item of every pair, as the solve's autotuner
-    # timed it with CUDA events for the configuration it chose (row direction: rows of C)
-    import ctypes
-    ms_r, ms_c = ctypes.c_float(0.0), ctypes.c_float(0.0)
-    kgrw = (ctypes.c_int32 * 4)()
-    _native.check(lib.wotg_batch_pass_timing(ctypes.byref(ms_r), ctypes.byref(ms_c), kgrw), 'wotg_batch_pass_timing')
     elems = float(sum(pairs[p].cost.I * pairs[p].cost.J for p, _ in items))
     pass_bytes = float(sum(4 * p.cost.I * p.cost.J for p in pairs))
     exp_pk = exp2_peak()

@@ -69,6 +69,29 @@ __device__ __forceinline__ void warp_lse(float& m, float& s) {
   }
 }
 
+// Merge of base-2 partials (m, s) in FP64 across a warp: every lane ends with
+// the warp's total as (m, S), value S 2^m (S in FP64).
+__device__ __forceinline__ void warp_lse_f64(float& m, double& S) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float m2 = __shfl_xor_sync(0xffffffffu, m, o);
+    const double S2 = __shfl_xor_sync(0xffffffffu, S, o);
+    const float mn = fmaxf(m, m2);
+    S = S * exp2((double)(m - mn)) + S2 * exp2((double)(m2 - mn));
+    m = mn;
+  }
+}
+
+// Compensated (Kahan) accumulation of v into (s, c): s - c carries the sum of
+// many FP32 terms with one rounding's error instead of one per term.
+// (Written with the _rn intrinsics so that no step is contracted into an FMA.)
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = __fsub_rn(v, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
 __device__ __forceinline__ double warp_sum(double x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);

@@ -193,8 +193,10 @@ __global__ void tc_bias_pack_kernel(int64_t n, int64_t n_pad, const double* __re
 //               (max, sum).
 // mbarriers hand buffers between roles (full / empty per B stage, per A buffer
 // and per accumulator). Every wait is bounded (wait_tries tries of up to 1 us):
-// a role that times out sets *err and a shared abort flag and stops, and the
-// other roles stop at their next wait. Before the CTA frees TMEM and exits,
+// a role that times out sets *err and a shared abort flag and stops; the
+// producer also stops at its next wait once the flag is set, and the other
+// roles' waits run out in turn (the hot waits of the MMA issuer and the
+// epilogue do not poll the flag). Before the CTA frees TMEM and exits,
 // whether it completed or gave up, the producer waits (with the full budget)
 // for every bulk copy it issued to land, and the MMA issuer commits once more
 // and waits until every MMA it issued has completed, so that no asynchronous
@@ -417,11 +419,10 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
           if (new_seg && j > 0) ++seg;
           if (new_seg)
             good = good &&
-                   tc::mbar_wait_or_abort(&a_full[seg % NA], (uint32_t)((seg / NA) & 1), wait_tries, abort_flag);
-          good = good && tc::mbar_wait_or_abort(&full[stage], (uint32_t)((j / S) & 1), wait_tries, abort_flag);
+                   tc::mbar_wait(&a_full[seg % NA], (uint32_t)((seg / NA) & 1), wait_tries);
+          good = good && tc::mbar_wait(&full[stage], (uint32_t)((j / S) & 1), wait_tries);
           if (j >= kTcAcc)
-            good = good && tc::mbar_wait_or_abort(&acc_empty[b], (uint32_t)((j / kTcAcc - 1) & 1), wait_tries,
-                                                  abort_flag);
+            good = good && tc::mbar_wait(&acc_empty[b], (uint32_t)((j / kTcAcc - 1) & 1), wait_tries);
           a_addr[u] = sA + (uint32_t)(seg % NA) * L::kTileBytes;
           b_addr[u] = sB + (uint32_t)stage * L::kTileBytes;
           d_addr[u] = tmem + (uint32_t)(128 * b);
@@ -477,7 +478,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
     for (int j = 0; j < n; ++j) {
       const int b = j % kTcAcc;
       const bool good = __all_sync(
-          0xffffffffu, tc::mbar_wait_or_abort(&acc_full[b], (uint32_t)((j / kTcAcc) & 1), wait_tries, abort_flag));
+          0xffffffffu, tc::mbar_wait(&acc_full[b], (uint32_t)((j / kTcAcc) & 1), wait_tries));
       if (!good) {
         if (lane == 0) {
           *abort_flag = 1;

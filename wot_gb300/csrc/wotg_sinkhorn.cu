@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const float* __restrict__
   for (int64_t i = warp; i < g.I; i += nwarps) {
     const float4* __restrict__ row = reinterpret_cast<const float4*>(C + i * g.ldc);
     const float o = PREC ? grid_offset(V.Lrow[i]) : 0.f;
-    float m = kNegBig, s = 0.f;
+    float m = kNegBig, s = 0.f, cmp = 0.f;   // PREC: compensated sum s - cmp
     int64_t k = lane;
     for (; k + 96 < nv; k += 128) {
       float4 cc[4], ww[4], wl[4];
@@ -183,7 +183,15 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const float* __restrict__
         const float x2 = expo<PREC>(cc[t].z, ww[t].z, wl[t].z, o, k2, k2l);
         const float x3 = expo<PREC>(cc[t].w, ww[t].w, wl[t].w, o, k2, k2l);
         const float mn = fmaxf(m, fmaxf(fmaxf(x0, x1), fmaxf(x2, x3)));
-        s = s * ex2(m - mn) + ((ex2(x0 - mn) + ex2(x1 - mn)) + (ex2(x2 - mn) + ex2(x3 - mn)));
+        const float r = ex2(m - mn);
+        const float v = (ex2(x0 - mn) + ex2(x1 - mn)) + (ex2(x2 - mn) + ex2(x3 - mn));
+        if (PREC) {
+          s = __fmul_rn(s, r);
+          cmp = __fmul_rn(cmp, r);
+          kahan_add(s, cmp, v);
+        } else {
+          s = s * r + v;
+        }
         m = mn;
       }
     }
@@ -196,12 +204,26 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const float* __restrict__
       const float x2 = expo<PREC>(cc.z, ww.z, wl.z, o, k2, k2l);
       const float x3 = expo<PREC>(cc.w, ww.w, wl.w, o, k2, k2l);
       const float mn = fmaxf(m, fmaxf(fmaxf(x0, x1), fmaxf(x2, x3)));
-      s = s * ex2(m - mn) + ((ex2(x0 - mn) + ex2(x1 - mn)) + (ex2(x2 - mn) + ex2(x3 - mn)));
+      const float r = ex2(m - mn);
+      const float v = (ex2(x0 - mn) + ex2(x1 - mn)) + (ex2(x2 - mn) + ex2(x3 - mn));
+      if (PREC) {
+        s = __fmul_rn(s, r);
+        cmp = __fmul_rn(cmp, r);
+        kahan_add(s, cmp, v);
+      } else {
+        s = s * r + v;
+      }
       m = mn;
     }
-    warp_lse(m, s);
+    double S = (double)s - (double)cmp;
+    if (PREC) {
+      warp_lse_f64(m, S);
+    } else {
+      warp_lse(m, s);
+      S = (double)s;
+    }
     if (lane == 0) {
-      const double L = ((double)o + (double)m + log2((double)s)) * kLn2;
+      const double L = ((double)o + (double)m + log2(S)) * kLn2;
       V.Lrow[i] = L;
       if (UPDATE_A) amax = fmax(amax, a_update(i, L, V, c));
     }
@@ -244,6 +266,7 @@ __global__ void __launch_bounds__(256) col_partial_kernel(const float* __restric
   }
   float m[4] = {kNegBig, kNegBig, kNegBig, kNegBig};
   float s[4] = {0.f, 0.f, 0.f, 0.f};
+  float cmp[4] = {0.f, 0.f, 0.f, 0.f};   // PREC: compensated sums s - cmp
   int64_t i = r0;
   for (; i + kColRowChunk <= r1; i += kColRowChunk) {
     float4 cc[kColRowChunk];
@@ -268,10 +291,17 @@ __global__ void __launch_bounds__(256) col_partial_kernel(const float* __restric
 #pragma unroll
       for (int t = 1; t < kColRowChunk; ++t) mx = fmaxf(mx, x[q][t]);
       const float mn = fmaxf(m[q], mx);
-      float acc = s[q] * ex2(m[q] - mn);
+      const float r = ex2(m[q] - mn);
+      float v = 0.f;
 #pragma unroll
-      for (int t = 0; t < kColRowChunk; ++t) acc += ex2(x[q][t] - mn);
-      s[q] = acc;
+      for (int t = 0; t < kColRowChunk; ++t) v += ex2(x[q][t] - mn);
+      if (PREC) {
+        s[q] = __fmul_rn(s[q], r);
+        cmp[q] = __fmul_rn(cmp[q], r);
+        kahan_add(s[q], cmp[q], v);
+      } else {
+        s[q] = s[q] * r + v;
+      }
       m[q] = mn;
     }
   }
@@ -284,9 +314,20 @@ __global__ void __launch_bounds__(256) col_partial_kernel(const float* __restric
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const float mn = fmaxf(m[q], xs[q]);
-      s[q] = s[q] * ex2(m[q] - mn) + ex2(xs[q] - mn);
+      const float r = ex2(m[q] - mn);
+      if (PREC) {
+        s[q] = __fmul_rn(s[q], r);
+        cmp[q] = __fmul_rn(cmp[q], r);
+        kahan_add(s[q], cmp[q], ex2(xs[q] - mn));
+      } else {
+        s[q] = s[q] * r + ex2(xs[q] - mn);
+      }
       m[q] = mn;
     }
+  }
+  if (PREC) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s[q] -= cmp[q];
   }
   float4* out = reinterpret_cast<float4*>(V.part + (int64_t)blockIdx.y * g.ldc + c4 * 4);
   out[0] = make_float4(m[0], s[0], m[1], s[1]);
@@ -301,12 +342,25 @@ __global__ void col_combine_kernel(Geom g, Vecs V, Coef c, int parity) {
   double bmax = 0.0;
   if (j < g.J) {
     const float o = PREC ? col_offset(V, g, j) : 0.f;
-    float m = kNegBig, s = 0.f;
-    for (int r = 0; r < g.nrb; ++r) {
-      const float2 ps = V.part[(int64_t)r * g.ldc + j];
-      lse_merge(m, s, ps.x, ps.y);
+    double L;
+    if (PREC) {
+      // the row-block partials merged in FP64 against their largest exponent
+      float m = kNegBig;
+      for (int r = 0; r < g.nrb; ++r) m = fmaxf(m, V.part[(int64_t)r * g.ldc + j].x);
+      double S = 0.0;
+      for (int r = 0; r < g.nrb; ++r) {
+        const float2 ps = V.part[(int64_t)r * g.ldc + j];
+        S += (double)ps.y * exp2((double)(ps.x - m));
+      }
+      L = ((double)o + (double)m + log2(S)) * kLn2;
+    } else {
+      float m = kNegBig, s = 0.f;
+      for (int r = 0; r < g.nrb; ++r) {
+        const float2 ps = V.part[(int64_t)r * g.ldc + j];
+        lse_merge(m, s, ps.x, ps.y);
+      }
+      L = ((double)m + log2((double)s)) * kLn2;
     }
-    const double L = ((double)o + (double)m + log2((double)s)) * kLn2;
     V.Lcol[j] = L;
     if (UPDATE_B) bmax = b_update(j, L, V, c);
   }
@@ -575,11 +629,11 @@ __device__ __forceinline__ double exp2_split(double t) {
 __global__ void __launch_bounds__(256) coupling_kernel(const float* __restrict__ C, Geom g, Vecs V,
                                                        Coef c, double log_scale, double* __restrict__ out) {
   const double k2 = c.kappa * kLog2e;
-  for (int64_t i = blockIdx.y; i < g.I; i += gridDim.y) {
-    const double wr = (V.u[i] * c.inv_eps + V.la[i] + log_scale) * kLog2e;
-    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.J;
-         j += (int64_t)gridDim.x * blockDim.x) {
-      const double wc = (V.v[j] * c.inv_eps + V.lb[j]) * kLog2e;
+  for (int64_t j0 = (int64_t)blockIdx.x * blockDim.x; j0 < g.J; j0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = j0 + threadIdx.x;
+    const double wc = j < g.J ? (V.v[j] * c.inv_eps + V.lb[j]) * kLog2e : 0.0;   // once per column
+    for (int64_t i = blockIdx.y; i < g.I && j < g.J; i += gridDim.y) {
+      const double wr = (V.u[i] * c.inv_eps + V.la[i] + log_scale) * kLog2e;
       out[i * g.J + j] = exp2_split(wr + wc - k2 * (double)C[i * g.ldc + j]);
     }
   }
@@ -853,7 +907,8 @@ struct Solver {
       WOTG_LAUNCHED();
     }
     if (tmap) {
-      dim3 grid((unsigned)std::min<int64_t>((g.J + 255) / 256, 16), (unsigned)std::min<int64_t>(g.I, 65535));
+      // every column in one wave of x blocks (its FP64 weight formed once per thread), rows over y
+      dim3 grid((unsigned)std::min<int64_t>((g.J + 255) / 256, 65535), (unsigned)std::min<int64_t>(g.I, 128));
       coupling_kernel<<<grid, 256, 0, st>>>(C, g, V, c, log_scale, tmap);
       WOTG_LAUNCHED();
     }
