@@ -1044,6 +1044,8 @@ static const PassCfg kCfgs[] = {
     {8, 2, pass_kernel<8, 2, true>, pass_kernel<8, 2, false>},
     {16, 1, pass_kernel<16, 1, true>, pass_kernel<16, 1, false>},
     {16, 2, pass_kernel<16, 2, true>, pass_kernel<16, 2, false>},
+    {8, 4, pass_kernel<8, 4, true>, pass_kernel<8, 4, false>},
+    {13, 2, pass_kernel<13, 2, true>, pass_kernel<13, 2, false>},
 };
 constexpr int kNumCfgs = sizeof(kCfgs) / sizeof(kCfgs[0]);
 
@@ -1078,8 +1080,8 @@ struct Layout {
   double* part;
   Item* items;
   Seg* segs;
-  Tile* tiles[2][2];  // [dir][rw - 1]
-  int ntiles[2][2];
+  Tile* tiles[2][3];  // [dir][rw_slot(rw)]
+  int ntiles[2][3];
   int *pair_items, *pair_off, *list_off, *row_n, *col_n, *chk_n, *counters, *active;
   Entry *row_list, *col_list, *chk_list;
   float* zeros;
@@ -1088,6 +1090,10 @@ struct Layout {
 };
 
 static inline int64_t round4(int64_t n) { return (n + 3) & ~int64_t(3); }
+
+// Rows per warp of a pass configuration (1, 2 or 4) -> its tile table.
+constexpr int kRowsPerWarp[3] = {1, 2, 4};
+static inline int rw_slot(int rw) { return rw == 4 ? 2 : rw - 1; }
 
 // Workspace layout; with base == nullptr only sizes. Fills host-side item
 // pointers when `host_items` is given.
@@ -1110,14 +1116,15 @@ static size_t layout(char* base, const wotg_pair* pairs, int np, const wotg_item
   }
   for (int k = 0; k < ni; ++k) kp[items[k].pair] += 1;
   for (int d = 0; d < 2; ++d)
-    for (int rw = 1; rw <= 2; ++rw) {
+    for (int sl = 0; sl < 3; ++sl) {
+      const int rw = kRowsPerWarp[sl];
       size_t n = 0;
       for (int p = 0; p < np; ++p) {
         const int rows = d == 0 ? rows0[p] : cols0[p];
         n += (size_t)((rows + 8 * rw - 1) / (8 * rw));
       }
-      L.ntiles[d][rw - 1] = (int)n;
-      L.tiles[d][rw - 1] = b.take<Tile>(n);
+      L.ntiles[d][sl] = (int)n;
+      L.tiles[d][sl] = b.take<Tile>(n);
     }
   L.pair_items = b.take<int>(ni);
   L.pair_off = b.take<int>(np + 1);
@@ -1219,7 +1226,7 @@ static int autotune(const Layout& L, const int* chk_off, int dir, int np, int ni
   int best_i = 0;
   int status = WOTG_OK;
   for (int c = 0; c < kNumCfgs && status == WOTG_OK; ++c) {
-    const PassArgs A{L.segs,    dir,      L.tiles[dir][kCfgs[c].rw - 1], L.ntiles[dir][kCfgs[c].rw - 1],
+    const PassArgs A{L.segs,    dir,      L.tiles[dir][rw_slot(kCfgs[c].rw)], L.ntiles[dir][rw_slot(kCfgs[c].rw)],
                      L.chk_n,   L.chk_list, chk_off, L.items, L.counters + 6};
     float t_min = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
@@ -1399,11 +1406,11 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
   // Upload tables (pageable host memory: these copies complete before return).
   WOTG_BCUDA(cudaMemcpyAsync(L.items, hi.data(), sizeof(Item) * ni, cudaMemcpyHostToDevice, cs));
   WOTG_BCUDA(cudaMemcpyAsync(L.segs, segs.data(), sizeof(Seg) * segs.size(), cudaMemcpyHostToDevice, cs));
-  std::vector<Tile> tiles[2][2];
+  std::vector<Tile> tiles[2][3];
   for (int d = 0; d < 2; ++d)
-    for (int rw = 1; rw <= 2; ++rw) {
-      tiles[d][rw - 1] = make_tiles(d == 0 ? rows0 : cols0, d == 0 ? cols0 : rows0, kp, 8 * rw);
-      WOTG_BCUDA(cudaMemcpyAsync(L.tiles[d][rw - 1], tiles[d][rw - 1].data(), sizeof(Tile) * tiles[d][rw - 1].size(),
+    for (int sl = 0; sl < 3; ++sl) {
+      tiles[d][sl] = make_tiles(d == 0 ? rows0 : cols0, d == 0 ? cols0 : rows0, kp, 8 * kRowsPerWarp[sl]);
+      WOTG_BCUDA(cudaMemcpyAsync(L.tiles[d][sl], tiles[d][sl].data(), sizeof(Tile) * tiles[d][sl].size(),
                                  cudaMemcpyHostToDevice, cs));
     }
   WOTG_BCUDA(cudaMemcpyAsync(L.pair_items, pair_items.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, cs));
@@ -1461,11 +1468,11 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
 
   const PassCfg& c0 = kCfgs[cfg[0]];
   const PassCfg& c1 = kCfgs[cfg[1]];
-  PassArgs Arow{L.segs, 0, L.tiles[0][c0.rw - 1], L.ntiles[0][c0.rw - 1], L.row_n, L.row_list, L.pair_off,
+  PassArgs Arow{L.segs, 0, L.tiles[0][rw_slot(c0.rw)], L.ntiles[0][rw_slot(c0.rw)], L.row_n, L.row_list, L.pair_off,
                 L.items, L.counters + 0};
-  PassArgs Acol{L.segs, 1, L.tiles[1][c1.rw - 1], L.ntiles[1][c1.rw - 1], L.col_n, L.col_list, L.pair_off,
+  PassArgs Acol{L.segs, 1, L.tiles[1][rw_slot(c1.rw)], L.ntiles[1][rw_slot(c1.rw)], L.col_n, L.col_list, L.pair_off,
                 L.items, L.counters + 1};
-  PassArgs Achk{L.segs, 0, L.tiles[0][c0.rw - 1], L.ntiles[0][c0.rw - 1], L.chk_n, L.chk_list, chk_off,
+  PassArgs Achk{L.segs, 0, L.tiles[0][rw_slot(c0.rw)], L.ntiles[0][rw_slot(c0.rw)], L.chk_n, L.chk_list, chk_off,
                 L.items, L.counters + 2};
   const int grid_row = pass_grid(c0.spec), grid_col = pass_grid(c1.spec);
 
