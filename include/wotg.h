@@ -239,6 +239,61 @@ int wotg_apply_coupling_f64(const double* X, int64_t I, int64_t J, const double*
                             int32_t transpose, int32_t normalize, double* out, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Products of the local PCA (wot/ot/util.py:240-255: scikit-learn's PCA of the
+ * double-centred genes x cells matrix of a day pair, whose randomized solver
+ * multiplies that matrix and its transpose with thin blocks of vectors and
+ * orthonormalises them). The expression matrix X (cells x genes, FP64) is taken
+ * in CSR form; the centrings enter the products as rank-one terms.
+ * ------------------------------------------------------------------------ */
+
+/* CSR of the dense row-major X (n x p, row stride ldx): wotg_csr_count writes
+ * rowptr (n + 1 int64: exclusive prefix sums of the row counts, rowptr[n] =
+ * nnz) and, if rowsum is not NULL, each row's sum (n FP64); wotg_csr_fill then
+ * writes colidx (int32) and vals (FP64) of nnz entries, ascending columns within
+ * each row. */
+int wotg_csr_count(const double* X, int64_t n, int64_t p, int64_t ldx, int64_t* rowptr, double* rowsum,
+                   void* stream);
+int wotg_csr_fill(const double* X, int64_t n, int64_t p, int64_t ldx, const int64_t* rowptr, int32_t* colidx,
+                  double* vals, void* stream);
+
+/* CSR of the transpose (p x n) of an n x p CSR matrix (p <= 32768), rows of
+ * each output row in increasing order (a stable counting sort, so that products
+ * with it sum in the same order on every run). */
+size_t wotg_csr_transpose_workspace_bytes(int64_t n, int64_t p);
+int wotg_csr_transpose(const int64_t* rowptr, const int32_t* colidx, const double* vals, int64_t n, int64_t p,
+                       int64_t* t_rowptr, int32_t* t_colidx, double* t_vals, void* workspace,
+                       size_t workspace_bytes, void* stream);
+
+/* Y (n x r) = X Q - 1 a^T - c b^T for the n-row CSR X and Q (rows x r, row-major),
+ * r <= 64; a, b (r) and c (n) may each be NULL (zero). With X the expression
+ * matrix, a = mu^T Q, b = 1^T Q and c the per-cell centring it is the product of
+ * the double-centred matrix the reference decomposes. */
+int wotg_spmm_centred(const int64_t* rowptr, const int32_t* colidx, const double* vals, int64_t n, const double* Q,
+                      int32_t r, const double* a, const double* c, const double* b, double* Y, void* stream);
+
+/* G (r x r) = A^T A of a dense row-major A (n x r), r <= 64 (the Gram matrix of
+ * the range finder's Cholesky QR), summed in a fixed order. */
+size_t wotg_gram_workspace_bytes(int64_t n, int32_t r);
+int wotg_gram_f64(const double* A, int64_t n, int32_t r, double* G, void* workspace, size_t workspace_bytes,
+                  void* stream);
+
+/* out (r) = w^T Q for w (K) and Q (K x r, row-major), r <= 64, summed in a fixed
+ * order (the rank-one centring terms mu^T Q, 1^T Q, c^T Q of the PCA products). */
+size_t wotg_vecmat_workspace_bytes(int64_t K, int32_t r);
+int wotg_vecmat_f64(const double* w, const double* Q, int64_t K, int32_t r, double* out, void* workspace,
+                    size_t workspace_bytes, void* stream);
+
+/* Dense FP64 product of two couplings for a long-range map:
+ *   C (M x N) = A (M x K) . B[b_rows] (K x N)
+ * row-major with leading dimensions lda >= K, ldb >= N, ldc >= N; row k of the
+ * right operand is row b_rows[k] of B (b_rows: K device int64 indices, or NULL
+ * for B itself). Replaces np.dot(tmap_0.X, tmap_1[tmap_0.var.index].X) of
+ * glue_transport_maps (wot/tmap/util.py:74-94), which chain_transport_maps
+ * applies along a path of day pairs (wot/tmap/chaining.py:4-40). */
+int wotg_gemm_f64(const double* A, int64_t lda, const double* B, int64_t ldb, const int64_t* b_rows, double* C,
+                  int64_t ldc, int64_t M, int64_t N, int64_t K, void* stream);
+
+/* ------------------------------------------------------------------------
  * Batched solves. The reference solves day pairs one after another
  * (OTModel.compute_all_transport_maps, wot/ot/ot_model.py:124-201, one
  * compute_transport_matrix per pair, ot_model.py:318) and a parameter sweep

@@ -88,3 +88,32 @@ def test_chained_pull_back_on_implicit_maps():
     fwd = np.array([p.p for p in model.push_forward(Population(0.0, np.ones(sizes[0]), 'all'), to_time=tp[-1],
                                                      as_list=True)])
     assert _rel(fwd, otm.push_forward(dense, tp, np.ones((1, sizes[0])), 0.0, tp[-1])) <= TOL
+
+
+@pytest.mark.parametrize('M,Nc,K', [(1, 1, 1), (65, 130, 17), (200, 70, 300), (3, 257, 64)])
+def test_gemm_f64_with_row_gather(M, Nc, K):
+    """wotg_gemm_f64 (the dense product of chained couplings) against NumPy FP64,
+    with the right operand's rows gathered by an index as glue_transport_maps does."""
+    import ctypes
+    import torch
+    from wot_gb300 import _native as N
+    rng = np.random.default_rng(M * 7 + Nc)
+    A = rng.random((M, K))
+    B = rng.random((K + 5, Nc))
+    rows = rng.permutation(K + 5)[:K]
+    out = torch.empty((M, Nc), dtype=torch.float64, device='cuda')
+    At, Bt = torch.as_tensor(A, device='cuda'), torch.as_tensor(B, device='cuda')
+    r = torch.as_tensor(rows.astype(np.int64), device='cuda')
+    st = N.load().wotg_gemm_f64(At.data_ptr(), K, Bt.data_ptr(), Nc, r.data_ptr(), out.data_ptr(), Nc, M, Nc, K,
+                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0
+    np.testing.assert_allclose(out.cpu().numpy(), A @ B[rows], rtol=1e-13, atol=0)
+
+
+def test_glue_rejects_cells_missing_from_the_next_map():
+    import wot_gb300 as wot
+    from wot_gb300.tmap.util import glue_transport_maps
+    t0 = wot.Dataset(np.ones((2, 3)), wot.Frame(index=['a', 'b']), wot.Frame(index=['x', 'y', 'z']))
+    t1 = wot.Dataset(np.ones((2, 2)), wot.Frame(index=['x', 'y']), wot.Frame(index=['p', 'q']))
+    with pytest.raises(KeyError):
+        glue_transport_maps(t0, t1)

@@ -38,7 +38,9 @@ EXPORTS = (
     'wotg_solve_batched', 'wotg_lse_matvec_multi_workspace_bytes', 'wotg_lse_matvec_multi',
     'wotg_coupling_from_potentials', 'wotg_ot_adjoint_workspace_bytes', 'wotg_ot_adjoint',
     'wotg_refine_potentials', 'wotg_exp2_rate', 'wotg_lse_points_timing', 'wotg_lse_points_bounded',
-    'wotg_batch_pass_timing',
+    'wotg_batch_pass_timing', 'wotg_gemm_f64', 'wotg_csr_count', 'wotg_csr_fill',
+    'wotg_csr_transpose_workspace_bytes', 'wotg_csr_transpose', 'wotg_spmm_centred', 'wotg_gram_workspace_bytes',
+    'wotg_gram_f64', 'wotg_vecmat_workspace_bytes', 'wotg_vecmat_f64',
 )
 
 
@@ -107,6 +109,16 @@ def load(path: str | None = None) -> ctypes.CDLL:
         'wotg_tc_selftest': (ctypes.c_int, [vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, i32, vp, vp]),
         'wotg_lse_points_workspace_bytes': (ctypes.c_size_t, [i64, i64, i32]),
         'wotg_lse_points': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, vp, vp, vp, ctypes.c_size_t, vp]),
+        'wotg_csr_count': (ctypes.c_int, [vp, i64, i64, i64, vp, vp, vp]),
+        'wotg_csr_fill': (ctypes.c_int, [vp, i64, i64, i64, vp, vp, vp, vp]),
+        'wotg_csr_transpose_workspace_bytes': (ctypes.c_size_t, [i64, i64]),
+        'wotg_csr_transpose': (ctypes.c_int, [vp, vp, vp, i64, i64, vp, vp, vp, vp, ctypes.c_size_t, vp]),
+        'wotg_spmm_centred': (ctypes.c_int, [vp, vp, vp, i64, vp, i32, vp, vp, vp, vp, vp]),
+        'wotg_gram_workspace_bytes': (ctypes.c_size_t, [i64, i32]),
+        'wotg_gram_f64': (ctypes.c_int, [vp, i64, i32, vp, vp, ctypes.c_size_t, vp]),
+        'wotg_vecmat_workspace_bytes': (ctypes.c_size_t, [i64, i32]),
+        'wotg_vecmat_f64': (ctypes.c_int, [vp, vp, i64, i32, vp, vp, ctypes.c_size_t, vp]),
+        'wotg_gemm_f64': (ctypes.c_int, [vp, i64, vp, i64, vp, vp, i64, i64, i64, i64, vp]),
         'wotg_batch_pass_timing': (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                                   ctypes.POINTER(ctypes.c_int32)]),
         'wotg_lse_points_bounded': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, vp, vp, ctypes.c_uint32,

@@ -84,13 +84,27 @@ class _Centred:
     """The reference's double-centred matrix as an operator, never formed:
     T = x - 1 mu^T - c 1^T (cells x genes; mu the gene means, c each cell's mean
     over genes after removing mu), i.e. the transpose of the matrix the
-    reference hands to scikit-learn. Products with T and T^T come from x (or
-    its sparse form) and two rank-one terms."""
+    reference hands to scikit-learn. Products with T and T^T come from x's
+    sparse form and two rank-one terms.
+
+    On the GPU (x a CUDA tensor, as compute_pca makes it) everything runs in
+    libwotg: the CSR of x and of its transpose (wotg_csr_count / _fill /
+    _transpose, a stable transpose so that every product sums in the same
+    order), the products with the rank-one centrings in their epilogue
+    (wotg_spmm_centred), the small vector-matrix products (wotg_gemm_f64). For a
+    CPU tensor the same operator is formed with torch's sparse products: that
+    branch exists for the CPU test suite, which checks the algorithm against
+    scikit-learn on a host without a GPU; compute_pca never takes it."""
 
     def __init__(self, x, mu, sparse=None):
         import torch
         self.x, self.mu = x, mu
         n, p = x.shape
+        self.n, self.p = n, p
+        self.device = x.is_cuda
+        if self.device:
+            self._build_device(x.contiguous(), mu.contiguous())
+            return
         self.c = (x @ torch.ones(p, dtype=x.dtype, device=x.device)) / p - float(mu.sum()) / p
         if sparse is None:
             sparse = int(torch.count_nonzero(x)) < SPARSE_DENSITY * x.numel()
@@ -101,6 +115,35 @@ class _Centred:
                 self.xs = x.to_sparse_csr()
                 self.xts = x.T.contiguous().to_sparse_csr()
 
+    def _build_device(self, x, mu):
+        import ctypes
+        import torch
+        lib, st = N.load(), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        n, p = self.n, self.p
+        f64 = dict(dtype=torch.float64, device='cuda')
+        rowptr = torch.empty(n + 1, dtype=torch.int64, device='cuda')
+        rowsum = torch.empty(n, **f64)
+        N.check(lib.wotg_csr_count(x.data_ptr(), n, p, x.stride(0), rowptr.data_ptr(), rowsum.data_ptr(), st),
+                'wotg_csr_count')
+        nnz = max(1, int(rowptr[n]))
+        colidx = torch.empty(nnz, dtype=torch.int32, device='cuda')
+        vals = torch.empty(nnz, **f64)
+        N.check(lib.wotg_csr_fill(x.data_ptr(), n, p, x.stride(0), rowptr.data_ptr(), colidx.data_ptr(),
+                                  vals.data_ptr(), st), 'wotg_csr_fill')
+        t_rowptr = torch.empty(p + 1, dtype=torch.int64, device='cuda')
+        t_colidx = torch.empty(nnz, dtype=torch.int32, device='cuda')
+        t_vals = torch.empty(nnz, **f64)
+        ws = torch.empty(lib.wotg_csr_transpose_workspace_bytes(n, p), dtype=torch.uint8, device='cuda')
+        N.check(lib.wotg_csr_transpose(rowptr.data_ptr(), colidx.data_ptr(), vals.data_ptr(), n, p,
+                                       t_rowptr.data_ptr(), t_colidx.data_ptr(), t_vals.data_ptr(), ws.data_ptr(),
+                                       ws.numel(), st), 'wotg_csr_transpose')
+        self.csr = (rowptr, colidx, vals)
+        self.csr_t = (t_rowptr, t_colidx, t_vals)
+        self.c = rowsum / p - float(mu.sum()) / p
+        self.ones_n = torch.ones(n, **f64)
+        self.ones_p = torch.ones(p, **f64)
+        self.mu = mu
+
     def _mm(self, a, b):
         import torch
         if a is None:
@@ -109,31 +152,87 @@ class _Centred:
             warnings.simplefilter('ignore', UserWarning)
             return torch.sparse.mm(a, b)
 
+    def _spmm(self, csr, rows, Q, a, c, b):
+        import ctypes
+        import torch
+        Y = torch.empty((rows, Q.shape[1]), dtype=torch.float64, device='cuda')
+        N.check(N.load().wotg_spmm_centred(csr[0].data_ptr(), csr[1].data_ptr(), csr[2].data_ptr(), rows,
+                                           Q.data_ptr(), Q.shape[1], a.data_ptr(), c.data_ptr(), b.data_ptr(),
+                                           Y.data_ptr(), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                'wotg_spmm_centred')
+        return Y
+
     def t_mul(self, Q):
         """T @ Q, Q genes x r."""
+        if self.device:
+            Q = Q.contiguous()
+            return self._spmm(self.csr, self.n, Q, vec_mat(self.mu, Q), self.c, vec_mat(self.ones_p, Q))
         xq = self._mm(self.xs, Q) if self.xs is not None else self.x @ Q
         return xq - (self.mu @ Q)[None, :] - self.c[:, None] * Q.sum(dim=0)[None, :]
 
     def tt_mul(self, Q):
         """T^T @ Q, Q cells x r."""
+        if self.device:
+            Q = Q.contiguous()
+            return self._spmm(self.csr_t, self.p, Q, vec_mat(self.c, Q), self.mu, vec_mat(self.ones_n, Q))
         xq = self._mm(self.xts, Q) if self.xts is not None else self.x.T @ Q
         return xq - self.mu[:, None] * Q.sum(dim=0)[None, :] - (self.c @ Q)[None, :]
 
 
+def mat_mul(A, B):
+    """A @ B of FP64 CUDA tensors in libwotg's GEMM kernel (wotg_gemm_f64)."""
+    import ctypes
+    import torch
+    A, B = A.contiguous(), B.contiguous()
+    M, K = A.shape
+    Nc = B.shape[1]
+    out = torch.empty((M, Nc), dtype=torch.float64, device='cuda')
+    N.check(N.load().wotg_gemm_f64(A.data_ptr(), K, B.data_ptr(), Nc, None, out.data_ptr(), Nc, M, Nc, K,
+                                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), 'wotg_gemm_f64')
+    return out
+
+
+def vec_mat(w, Q):
+    """w^T Q (a vector of Q's width) for FP64 CUDA tensors, in libwotg's
+    vector-matrix kernel (fixed-order sums over Q's long dimension)."""
+    import ctypes
+    import torch
+    w, Q = w.contiguous(), Q.contiguous()
+    K, r = Q.shape
+    lib = N.load()
+    out = torch.empty(r, dtype=torch.float64, device='cuda')
+    ws = torch.empty(lib.wotg_vecmat_workspace_bytes(K, r), dtype=torch.uint8, device='cuda')
+    N.check(lib.wotg_vecmat_f64(w.data_ptr(), Q.data_ptr(), K, r, out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), 'wotg_vecmat_f64')
+    return out
+
+
 def _orthonormal(A):
-    """An orthonormal basis of A's columns: Cholesky QR twice, the r x r
-    factorisations on the host; Householder QR on the host when A's Gram
-    matrix is not positive definite (rank-deficient iterates)."""
+    """An orthonormal basis of A's columns: Cholesky QR twice, A^T A and the
+    product with R^-1 on the device (libwotg's Gram and GEMM kernels for CUDA
+    tensors), the r x r factorisations on the host; Householder QR on the host
+    when A's Gram matrix is not positive definite (rank-deficient iterates)."""
+    import ctypes
     import torch
     for _ in range(2):
-        G = (A.T @ A).cpu().numpy()
+        if A.is_cuda:
+            A = A.contiguous()
+            n, r = A.shape
+            lib = N.load()
+            G = torch.empty((r, r), dtype=torch.float64, device='cuda')
+            ws = torch.empty(lib.wotg_gram_workspace_bytes(n, r), dtype=torch.uint8, device='cuda')
+            N.check(lib.wotg_gram_f64(A.data_ptr(), n, r, G.data_ptr(), ws.data_ptr(), ws.numel(),
+                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)), 'wotg_gram_f64')
+            G = G.cpu().numpy()
+        else:
+            G = (A.T @ A).cpu().numpy()
         try:
             L = np.linalg.cholesky(G)
         except np.linalg.LinAlgError:
             q, _ = np.linalg.qr(A.cpu().numpy())
             return torch.as_tensor(q, device=A.device)
-        Rinv = np.linalg.inv(L.T)
-        A = A @ torch.as_tensor(Rinv, dtype=A.dtype, device=A.device)
+        Rinv = torch.as_tensor(np.linalg.inv(L.T), dtype=A.dtype, device=A.device)
+        A = mat_mul(A, Rinv) if A.is_cuda else A @ Rinv
     return A
 
 
@@ -163,7 +262,8 @@ def reference_pca(x, mu, n_components, seed=58951, n_oversamples=10, sparse=None
     B = tmul(Q).T                # r x cols = Q^T M
     Uh, s, Vt = np.linalg.svd(B.cpu().numpy(), full_matrices=False)
     if transpose:
-        comp = Q @ torch.as_tensor(Uh[:, :k], dtype=x.dtype, device=x.device)     # cells x k
+        U_k = torch.as_tensor(np.ascontiguousarray(Uh[:, :k]), dtype=x.dtype, device=x.device)
+        comp = mat_mul(Q, U_k) if x.is_cuda else Q @ U_k                            # cells x k
     else:
         comp = torch.as_tensor(Vt[:k].T.copy(), dtype=x.dtype, device=x.device)  # cells x k
     return _largest_entry_positive(comp), torch.as_tensor(s[:k], dtype=x.dtype, device=x.device), solver
