@@ -211,6 +211,21 @@ int wotg_lse_points_bounded(const float* X, int64_t I, int64_t ldx, const float*
                             int32_t d, double scale, const double* w, double* L, uint32_t wait_tries,
                             void* workspace, size_t workspace_bytes, void* stream);
 
+/* A coupling held as potentials applied to k populations at once, on the
+ * tensor cores with one exp per (i, j) for all of them:
+ *   out[p * I + i] = exp(bias_i) sum_j exp(w[j] - scale |x_i - y_j|^2) P[p * ldp + j],  p < k
+ * X (I x d), Y (J x d) FP32 points (d <= 62), w (J) and bias (I, may be NULL) FP64,
+ * P FP64 k rows of ldp >= J weights (populations), out FP64 k x I, all on the
+ * device. With w = v_bar / eps, bias = u_bar / eps + log scale and the
+ * coupling's cost scale over eps it is the pull-back (tmap @ P.T).T of
+ * transport_map_model.py:356 (push_forward, :290, with the roles of the two
+ * point sets exchanged), for a map tmap = exp((u_bar + v_bar - C) / eps) scale
+ * that is never formed. The populations go through the kernel eight at a time. */
+size_t wotg_apply_points_workspace_bytes(int64_t I, int64_t J, int32_t d);
+int wotg_apply_points(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy, int32_t d,
+                      double scale, const double* w, const double* bias, const double* P, int64_t ldp, int32_t k,
+                      double* out, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Diagnostic (no counterpart in the reference): the mean device time of the
  * tensor-core kernel of wotg_lse_points alone (no packing, no finish), over
  * n_launch back-to-back launches timed with CUDA events on `stream`. With

@@ -117,3 +117,35 @@ def test_glue_rejects_cells_missing_from_the_next_map():
     t1 = wot.Dataset(np.ones((2, 2)), wot.Frame(index=['x', 'y']), wot.Frame(index=['p', 'q']))
     with pytest.raises(KeyError):
         glue_transport_maps(t0, t1)
+
+
+@pytest.mark.parametrize('d,k', [(30, 11), (50, 3), (3, 1)])
+def test_apply_points_populations_vs_fp64(d, k):
+    """wotg_apply_points: k populations through a coupling held as potentials,
+    one exp per entry for all of them (eight per launch: 11 takes two), against
+    the same sums in FP64: real-valued, indicator and all-zero populations."""
+    from wot_gb300 import synthetic
+    from wot_gb300.ot import device as D
+    I, J = 700, 900
+    x = synthetic.gaussian_mixture_points(I, d=d, seed=d)
+    y = synthetic.gaussian_mixture_points(J, d=d, seed=d + 1)
+    rng = np.random.default_rng(k)
+    C = ((x.astype(np.float64)[:, None, :] - y.astype(np.float64)[None, :, :]) ** 2).sum(-1)
+    scale = 1.0 / (np.median(C) * 0.05)
+    w = rng.normal(size=J) * 3
+    b = rng.normal(size=I)
+    P = rng.random((k, J))
+    P[0] = (P[0] < 0.1)
+    if k > 2:
+        P[2] = 0.0
+    out = D.apply_points(x, y, w, b, P, scale).cpu().numpy()
+    z = w[None, :] - scale * C
+    m = z.max(axis=1, keepdims=True)
+    E = np.exp(z - m)
+    ref = np.exp(b[:, None] + m) * (E @ P.T)          # I x k
+    ref = ref.T
+    for p in range(k):
+        if np.abs(ref[p]).max() == 0:
+            assert np.all(out[p] == 0)
+        else:
+            assert _rel(out[p], ref[p]) <= 1e-4, (p, _rel(out[p], ref[p]))

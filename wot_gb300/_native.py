@@ -40,7 +40,8 @@ EXPORTS = (
     'wotg_refine_potentials', 'wotg_exp2_rate', 'wotg_lse_points_timing', 'wotg_lse_points_bounded',
     'wotg_batch_pass_timing', 'wotg_gemm_f64', 'wotg_csr_count', 'wotg_csr_fill',
     'wotg_csr_transpose_workspace_bytes', 'wotg_csr_transpose', 'wotg_spmm_centred', 'wotg_gram_workspace_bytes',
-    'wotg_gram_f64', 'wotg_vecmat_workspace_bytes', 'wotg_vecmat_f64',
+    'wotg_gram_f64', 'wotg_vecmat_workspace_bytes', 'wotg_vecmat_f64', 'wotg_apply_points_workspace_bytes',
+    'wotg_apply_points',
 )
 
 
@@ -118,6 +119,9 @@ def load(path: str | None = None) -> ctypes.CDLL:
         'wotg_gram_f64': (ctypes.c_int, [vp, i64, i32, vp, vp, ctypes.c_size_t, vp]),
         'wotg_vecmat_workspace_bytes': (ctypes.c_size_t, [i64, i32]),
         'wotg_vecmat_f64': (ctypes.c_int, [vp, vp, i64, i32, vp, vp, ctypes.c_size_t, vp]),
+        'wotg_apply_points_workspace_bytes': (ctypes.c_size_t, [i64, i64, i32]),
+        'wotg_apply_points': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, vp, vp, vp, i64, i32, vp, vp,
+                                             ctypes.c_size_t, vp]),
         'wotg_gemm_f64': (ctypes.c_int, [vp, i64, vp, i64, vp, vp, i64, i64, i64, i64, vp]),
         'wotg_batch_pass_timing': (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                                   ctypes.POINTER(ctypes.c_int32)]),

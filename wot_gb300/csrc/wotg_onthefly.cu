@@ -293,12 +293,46 @@ __device__ __forceinline__ void sum32_off(const float (&d)[32], float o, float& 
   s += e[0].x + e[0].y;
 }
 
-template <int KP>
+// Weighted sums of 32 exponents for up to NPOP populations at once (the
+// population form of the epilogue): one exp2 per element against the running
+// maximum m, then s[k] += 2^(d - m) w[k][col] for every population k, the
+// weights w (npop rows of ldw floats, 16-byte aligned) read as warp-uniform
+// 128-bit loads. The sums are rescaled when the maximum moves.
+template <int NPOP>
+__device__ __forceinline__ void multi32(const float (&d)[32], const float* __restrict__ w, int npop, int ldw,
+                                        int col0, float& m, float (&s)[NPOP]) {
+  float mx = d[0];
+#pragma unroll
+  for (int c = 1; c < 32; ++c) mx = fmaxf(mx, d[c]);
+  const float mn = fmaxf(m, mx);
+  const float r = ex2(m - mn);
+#pragma unroll
+  for (int k = 0; k < NPOP; ++k) s[k] *= r;
+  m = mn;
+#pragma unroll
+  for (int c = 0; c < 32; c += 4) {
+    const float e0 = ex2(d[c] - mn), e1 = ex2(d[c + 1] - mn), e2 = ex2(d[c + 2] - mn), e3 = ex2(d[c + 3] - mn);
+#pragma unroll
+    for (int k = 0; k < NPOP; ++k) {
+      if (k < npop) {
+        const float4 pw = __ldg(reinterpret_cast<const float4*>(w + (int64_t)k * ldw + col0 + c));
+        s[k] = fmaf(e0, pw.x, fmaf(e1, pw.y, fmaf(e2, pw.z, fmaf(e3, pw.w, s[k]))));
+      }
+    }
+  }
+}
+
+// NPOP = 0: the log-sum-exp half-step (partials (m, s) in part). NPOP > 0: the
+// population form, npop <= NPOP weighted sums per row (maxima in part[].x,
+// sums in psum[slot * NPOP + k]) with the population weights popw.
+template <int KP, int NPOP>
 __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const __half* __restrict__ Pt,
                                                                const __half* __restrict__ Qt,
                                                                int n_pt, int nq, float2* __restrict__ part,
                                                                const float* __restrict__ off,
-                                                               int* __restrict__ err, uint32_t wait_tries) {
+                                                               int* __restrict__ err, uint32_t wait_tries,
+                                                               const float* __restrict__ popw, int npop,
+                                                               int ldpw, float* __restrict__ psum) {
   using L = TcSmem<KP>;
   constexpr int S = L::kStages;
   extern __shared__ unsigned char smem_raw[];
@@ -472,6 +506,9 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
     const int wq = warp & 3, cq = (warp - 2) >> 2;
     const int row = 32 * wq + lane;
     float m = kNegBig, s = 0.f;
+    float sp[NPOP > 0 ? NPOP : 1];
+#pragma unroll
+    for (int k = 0; k < (NPOP > 0 ? NPOP : 1); ++k) sp[k] = 0.f;
     int t = t_first, q = q_first;
     // speculative form: the row's offset for the current row tile
     if (off) m = off[(int64_t)t * 128 + row];
@@ -495,7 +532,10 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
       tc::tmem_wait_ld();
       tc::tmem_hold(d0);
       tc::tmem_ld32(taddr + 32, d1);
-      if (off)
+      const int col0 = q * 128 + kTcColsPerWarp * cq;   // first column of d0 within the column set
+      if constexpr (NPOP > 0)
+        multi32<NPOP>(d0, popw, npop, ldpw, col0, m, sp);
+      else if (off)
         sum32_off(d0, m, s);
       else
         lse32(d0, m, s);
@@ -504,12 +544,22 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
-      if (off)
+      if constexpr (NPOP > 0)
+        multi32<NPOP>(d1, popw, npop, ldpw, col0 + 32, m, sp);
+      else if (off)
         sum32_off(d1, m, s);
       else
         lse32(d1, m, s);
       if (++q == nq || j == n - 1) {
-        part[(((int64_t)blockIdx.x + t) * 128 + row) * kTcParts + cq] = make_float2(m, s);
+        const int64_t slot = (((int64_t)blockIdx.x + t) * 128 + row) * kTcParts + cq;
+        part[slot] = make_float2(m, s);
+        if constexpr (NPOP > 0) {
+#pragma unroll
+          for (int k = 0; k < NPOP; ++k) {
+            psum[slot * NPOP + k] = sp[k];
+            sp[k] = 0.f;
+          }
+        }
         m = kNegBig;
         s = 0.f;
         if (q == nq) {
@@ -543,10 +593,10 @@ int tc_pack_bias(int64_t n, const double* pot, const double* lsc, const double* 
   return WOTG_OK;
 }
 
-template <int KP>
+template <int KP, int NPOP = 0>
 static cudaError_t tc_set_smem_attr() {
-  static cudaError_t once = cudaFuncSetAttribute(lse_tc_kernel<KP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)TcSmem<KP>::kAlloc);
+  static cudaError_t once = cudaFuncSetAttribute(lse_tc_kernel<KP, NPOP>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TcSmem<KP>::kAlloc);
   return once;
 }
 
@@ -561,12 +611,12 @@ int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int 
                   const float* off, int* err, cudaStream_t st, uint32_t wait_tries) {
   if (kp == 32) {
     WOTG_CUDA(tc_set_smem_attr<32>());
-    lse_tc_kernel<32><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
-                                                                     wait_tries);
+    lse_tc_kernel<32, 0><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
+                                                                        wait_tries, nullptr, 0, 0, nullptr);
   } else if (kp == 64) {
     WOTG_CUDA(tc_set_smem_attr<64>());
-    lse_tc_kernel<64><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
-                                                                     wait_tries);
+    lse_tc_kernel<64, 0><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
+                                                                        wait_tries, nullptr, 0, 0, nullptr);
   } else {
     return WOTG_BADARG;
   }
@@ -594,6 +644,47 @@ __global__ void lse_points_finish_kernel(int64_t n, int nq, int ctas, int nparts
   const double D = (double)m + log2((double)s);
   if (L) L[i] = D * kLn2 - scale * norm[i];
   if (off) off[i] = (float)D;
+}
+
+// Population weights of columns [0, J) of k populations (FP64, row stride ldp),
+// from population k0 on, as FP32 rows of jpad entries (zero past J).
+__global__ void pop_pack_kernel(const double* __restrict__ P, int64_t ldp, int k0, int k, int64_t J, int64_t jpad,
+                                int npop_max, float* __restrict__ popw) {
+  const int64_t total = (int64_t)npop_max * jpad;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int kk = (int)(idx / jpad);
+    const int64_t j = idx % jpad;
+    popw[idx] = (kk < k && j < J) ? (float)P[(int64_t)(k0 + kk) * ldp + j] : 0.f;
+  }
+}
+
+// Finish of the population form: per row, the partials of every CTA range
+// merged in FP64 against their largest maximum, then
+// out[(k0 + kk) * n + i] = exp(b_i - scale |x_i|^2) 2^M S_kk.
+__global__ void pop_finish_kernel(int64_t n, int nq, int ctas, int nparts, const float2* __restrict__ part,
+                                  const float* __restrict__ psum, int npop_max, int k0, int k,
+                                  const double* __restrict__ norm, double scale, const double* __restrict__ b,
+                                  double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t t = i >> 7;
+  const int64_t total = ((n + 127) >> 7) * (int64_t)nq;
+  const int64_t c_lo = tc_cta_of(t * nq, total, ctas);
+  const int64_t c_hi = tc_cta_of((t + 1) * nq - 1, total, ctas);
+  float M = kNegBig;
+  for (int64_t cc = c_lo; cc <= c_hi; ++cc)
+    for (int q = 0; q < nparts; ++q) M = fmaxf(M, part[((cc + t) * 128 + (i & 127)) * nparts + q].x);
+  const double base = (double)M * kLn2 - scale * norm[i] + (b ? b[i] : 0.0);
+  for (int kk = 0; kk < k; ++kk) {
+    double S = 0.0;
+    for (int64_t cc = c_lo; cc <= c_hi; ++cc)
+      for (int q = 0; q < nparts; ++q) {
+        const int64_t slot = ((cc + t) * 128 + (i & 127)) * nparts + q;
+        S += (double)psum[slot * npop_max + kk] * exp2((double)(part[slot].x - M));
+      }
+    out[(int64_t)(k0 + kk) * n + i] = S > 0.0 ? exp(base + log(S)) : 0.0;
+  }
 }
 
 struct PointsLayout {
@@ -751,5 +842,72 @@ extern "C" int wotg_lse_points_timing(const float* X, int64_t I, int64_t ldx, co
     return WOTG_CUDA_ERROR;
   }
   *ms_per_launch = ms / (float)n_launch;
+  return WOTG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The population form: out[k, i] = exp(b_i) sum_j exp(w_j - scale |x_i - y_j|^2) P[k, j]
+// with one exp per (i, j) for up to kTcPops populations per launch.
+// ---------------------------------------------------------------------------
+namespace wotg {
+constexpr int kTcPops = 8;
+
+static size_t apply_layout(Bump& b, int64_t I, int64_t J, int d, PointsLayout& P, float** popw, float** psum) {
+  points_layout(b, I, J, d, P);
+  *popw = b.take<float>((size_t)kTcPops * P.n_yt * 128);
+  *psum = b.take<float>((size_t)(P.ctas + P.n_xt) * 128 * kTcParts * kTcPops);
+  return b.off + 256;
+}
+}  // namespace wotg
+
+extern "C" size_t wotg_apply_points_workspace_bytes(int64_t I, int64_t J, int32_t d) {
+  if (I <= 0 || J <= 0 || d < 1 || d > tc_max_dim()) return 0;
+  Bump b{nullptr, 0};
+  PointsLayout P{};
+  float *popw, *psum;
+  return apply_layout(b, I, J, d, P, &popw, &psum);
+}
+
+extern "C" int wotg_apply_points(const float* X, int64_t I, int64_t ldx, const float* Y, int64_t J, int64_t ldy,
+                                 int32_t d, double scale, const double* w, const double* bias, const double* Pw,
+                                 int64_t ldp, int32_t k, double* out, void* workspace, size_t workspace_bytes,
+                                 void* stream) {
+  if (!X || !Y || !w || !Pw || !out || I <= 0 || J <= 0 || d < 1 || d > tc_max_dim() || ldx < d || ldy < d ||
+      !(scale > 0) || k < 1 || ldp < J)
+    return WOTG_BADARG;
+  if (!workspace || workspace_bytes < wotg_apply_points_workspace_bytes(I, J, d)) return WOTG_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  Bump b{reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255)), 0};
+  PointsLayout P{};
+  float *popw, *psum;
+  apply_layout(b, I, J, d, P, &popw, &psum);
+  const double sigma = std::sqrt(scale);
+  const int64_t jpad = (int64_t)P.n_yt * 128;
+  WOTG_CUDA(cudaMemsetAsync(P.err, 0, sizeof(int), st));
+  int s = tc_pack_points(X, I, ldx, d, P.kp, (float)(2.0 * kLog2e * sigma), 1, P.Xa, P.normX, st);
+  if (s) return s;
+  s = tc_pack_points(Y, J, ldy, d, P.kp, (float)sigma, 0, P.Yb, P.normY, st);
+  if (s) return s;
+  s = tc_pack_bias(J, w, nullptr, P.normY, 1.0, scale * kLog2e, d, P.kp, P.Yb, st);
+  if (s) return s;
+  for (int k0 = 0; k0 < k; k0 += kTcPops) {
+    const int kc = std::min(kTcPops, k - k0);
+    const int pgrid = (int)std::min<int64_t>((kTcPops * jpad + 255) / 256, (int64_t)sm_count() * 8);
+    pop_pack_kernel<<<pgrid, 256, 0, st>>>(Pw, ldp, k0, kc, J, jpad, kTcPops, popw);
+    WOTG_LAUNCHED();
+    if (P.kp == 32) {
+      WOTG_CUDA((tc_set_smem_attr<32, kTcPops>()));
+      lse_tc_kernel<32, kTcPops><<<P.ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(
+          P.Xa, P.Yb, P.n_xt, P.n_yt, P.part, nullptr, P.err, kTcWaitTries, popw, kc, (int)jpad, psum);
+    } else {
+      WOTG_CUDA((tc_set_smem_attr<64, kTcPops>()));
+      lse_tc_kernel<64, kTcPops><<<P.ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(
+          P.Xa, P.Yb, P.n_xt, P.n_yt, P.part, nullptr, P.err, kTcWaitTries, popw, kc, (int)jpad, psum);
+    }
+    WOTG_LAUNCHED();
+    pop_finish_kernel<<<(unsigned)((I + 255) / 256), 256, 0, st>>>(I, P.n_yt, P.ctas, kTcParts, P.part, psum,
+                                                                  kTcPops, k0, kc, P.normX, scale, bias, out);
+    WOTG_LAUNCHED();
+  }
   return WOTG_OK;
 }

@@ -288,6 +288,30 @@ def lse_points(x, y, w, scale: float):
     return L
 
 
+def apply_points(x, y, w, bias, P, scale: float):
+    """out[k, i] = exp(bias_i) sum_j exp(w_j - scale |x_i - y_j|^2) P[k, j] on the
+    tensor cores, one exp per (i, j) for all rows of P (FP64 k x I out)."""
+    torch = _torch()
+    X = _dev_f32(x, torch)
+    Y = _dev_f32(y, torch)
+    W = _dev_f64(w, torch).reshape(-1)
+    B = _dev_f64(bias, torch).reshape(-1)
+    Pd = _dev_f64(P, torch)
+    I, d = X.shape
+    J = Y.shape[0]
+    k = Pd.shape[0]
+    lib = N.load()
+    nbytes = lib.wotg_apply_points_workspace_bytes(I, J, d)
+    if nbytes == 0:
+        raise ValueError('invalid points for the on-the-fly form (d <= 62)')
+    ws = torch.empty(nbytes, dtype=torch.uint8, device='cuda')
+    out = torch.empty((k, I), dtype=torch.float64, device='cuda')
+    N.check(lib.wotg_apply_points(X.data_ptr(), I, X.stride(0), Y.data_ptr(), J, Y.stride(0), d, float(scale),
+                                  W.data_ptr(), B.data_ptr(), Pd.data_ptr(), Pd.stride(0), k, out.data_ptr(),
+                                  ws.data_ptr(), nbytes, _stream()), 'wotg_apply_points')
+    return out
+
+
 def transpose_cost(cost: DeviceCost):
     """C^T (J x ldct FP32, +inf padding) of a device cost; the column form a batch reads."""
     torch = _torch()

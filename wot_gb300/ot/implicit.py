@@ -10,12 +10,14 @@ and applies the map to populations without forming it:
         out_i = exp(u_bar_i/eps + log scale) sum_j exp(v_bar_j/eps + log p_j - s c_ij/eps)
     push forward  p @ tmap      (transport_map_model.py:290)
         out_j = exp(v_bar_j/eps + log scale) sum_i exp(u_bar_i/eps + log p_i - s c_ij/eps)
-i.e. one log-sum-exp half-step per population: on the tensor cores from the
-points (``wotg_lse_points``, the cost recomputed tile by tile) when the points
-are held (at most 62 dimensions), else on the materialised cost or its
-transpose (``wotg_lse_matvec_multi``, every population in one pass; built from
-the points for the call when they have more dimensions). A 60000 x 60000 map
-costs 1 MB of potentials instead of 28.8 GB of FP64.
+on the tensor cores from the points (``wotg_apply_points``: the cost recomputed
+tile by tile, one exp per entry shared by every population, the populations'
+weights applied in the epilogue) when the points are held (at most 62
+dimensions), else as one log-sum-exp half-step per population on the
+materialised cost or its transpose (``wotg_lse_matvec_multi``, every
+population in one pass; built from the points for the call when they have more
+dimensions). A 60000 x 60000 map costs 1 MB of potentials instead of 28.8 GB
+of FP64.
 """
 from __future__ import annotations
 
@@ -71,20 +73,19 @@ class ImplicitCoupling:
         if src_pts is None and C is None:
             raise ValueError('this implicit coupling holds neither points nor the cost for this direction')
         inv_eps = 1.0 / self.eps
-        W = tgt_pot.reshape(1, -1) * inv_eps + torch.log(P)            # natural log weights, k x cols
         if C is None and src_pts.shape[1] > D.TC_MAX_DIM:
             # too many dimensions for the tensor-core packing: this direction's cost from the points
             c = D.cost_from_points(src_pts, tgt_pts)
             C, ldc = c.C, c.ldc
         if src_pts is not None and C is None:
-            L = torch.stack([D.lse_points(src_pts, tgt_pts, W[k], self.cost_scale * inv_eps)
-                             for k in range(W.shape[0])])
-        else:
-            ldw = N.round_up(cols, 4)
-            W2 = torch.zeros((W.shape[0], ldw), dtype=torch.float32, device='cuda')
-            W2[:, :cols] = W * LOG2E
-            k2 = self.cost_scale * inv_eps * LOG2E
-            L = D.lse_multi(C, rows, cols, ldc, W2, [k2] * W.shape[0])
+            return D.apply_points(src_pts, tgt_pts, tgt_pot * inv_eps, src_pot * inv_eps + self.log_scale, P,
+                                  self.cost_scale * inv_eps)
+        W = tgt_pot.reshape(1, -1) * inv_eps + torch.log(P)            # natural log weights, k x cols
+        ldw = N.round_up(cols, 4)
+        W2 = torch.zeros((W.shape[0], ldw), dtype=torch.float32, device='cuda')
+        W2[:, :cols] = W * LOG2E
+        k2 = self.cost_scale * inv_eps * LOG2E
+        L = D.lse_multi(C, rows, cols, ldc, W2, [k2] * W.shape[0])
         return torch.exp(L + src_pot.reshape(1, -1) * inv_eps + self.log_scale)
 
     def pull_back(self, P, normalize=True):
