@@ -175,18 +175,21 @@ def cpu_sample(a, b, G, I_s, J_s, rng, stages=None):
     return time.perf_counter() - t0, iters[0], T, (a_s, b_s, G_s)
 
 
-def dev_errors(T, R):
+def dev_errors(T, R, block=4096):
     """Parity of a device coupling T with the FP64 reference R (torch tensors):
     max|T - R| / max|R|; max |T - R| / |R| over the entries |R| >= 1e-6 max|R|;
-    the row and column marginals' max |r - r_ref| / max r_ref."""
+    the row and column marginals' max |r - r_ref| / max r_ref. Row blocks keep
+    the temporaries small for 60000 x 60000 maps."""
     import torch
-    T = T.to(torch.float64)
-    mx = R.abs().max()
-    d = (T - R).abs()
-    ce = float(d.max() / mx)
-    keep = R.abs() >= 1e-6 * mx
-    ee = float((d[keep] / R.abs()[keep]).max())
-    del d, keep
+    mx = float(R.abs().max())
+    ce = ee = 0.0
+    for r0 in range(0, R.shape[0], block):
+        Rb, Tb = R[r0:r0 + block], T[r0:r0 + block].to(torch.float64)
+        d = (Tb - Rb).abs()
+        ce = max(ce, float(d.max()) / mx)
+        keep = Rb.abs() >= 1e-6 * mx
+        if bool(keep.any()):
+            ee = max(ee, float((d[keep] / Rb.abs()[keep]).max()))
     rr, rc = R.sum(1), R.sum(0)
     me = max(float((T.sum(1) - rr).abs().max() / rr.abs().max()), float((T.sum(0) - rc).abs().max() / rc.abs().max()))
     return {'coupling_max_rel_err': ce, 'element_max_rel_err': ee, 'marginal_max_rel_err': me}
@@ -532,7 +535,7 @@ def course_e2e(days, sizes):
     expression (host FP32), OTModel(...).compute_transport_maps_batched over
     the consecutive pairs x the 5 x 5 sweep (device PCA, cost and median per
     pair, the batched solve), then every map's potentials read back to the
-    host. One timed call after one untimed call."""
+    host. One timed call."""
     import torch
     import wot_gb300 as wot
     X = np.vstack([d[0] for d in days])
@@ -547,7 +550,7 @@ def course_e2e(days, sizes):
         host = {k: (m.u_bar.cpu().numpy(), m.v_bar.cpu().numpy()) for k, m in maps.items()}
         return maps, host
 
-    call()
+    # one timed call (the kernels and the batch's autotuning are warm from the device-resident runs)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     maps, host = call()
@@ -678,6 +681,17 @@ def run_chain(args, data):
     u_fix = eps * a1 * (torch.log(G[rows]) - lse)
     resid = float((u_fix - big.u_bar[rows]).abs().max() / big.u_bar.abs().max())
     del cost, C_rows
+    parity_full = None
+    if not getattr(args, 'no_parity', False):
+        # the whole map against the reference's solver in FP64 (oracle/torch_ot.py, row blocks)
+        torch.cuda.empty_cache()
+        R, it_ref, t_ref = fp64_reference(a, b, G, CHAIN_CFG)
+        T = big.dense()
+        parity_full = dict(dev_errors(T, R), shape=[sizes[0], sizes[1]], iterations_gpu=iters // args.steps,
+                           iterations_oracle=it_ref, oracle_s=t_ref,
+                           oracle='the reference solver restated in FP64 on the GPU (oracle/torch_ot.py)')
+        del R, T
+        torch.cuda.empty_cache()
 
     # the chain: 20 maps held as potentials
     chain = []
@@ -737,7 +751,7 @@ def run_chain(args, data):
                        'timed': 'cost (for the exact median) + median + duality-gap solve, potentials out'},
             'sinkhorn_iter_per_s': iters / args.steps / t, 'iterations_per_map': iters / args.steps,
             'element_evaluations_per_s': 2.0 * sizes[0] * sizes[1] * iters / args.steps / t,
-            'fixed_point_residual_sampled_rows': resid,
+            'fixed_point_residual_sampled_rows': resid, 'parity_full': parity_full,
             'chain': {'maps': len(chain), 'cells': sizes[2:], 'solve_s': t_chain, 'iterations': chain_iters,
                       'pull_back_s': t_pull, 'populations': 8,
                       'pull_back_entries_per_s': chain_elems / t_pull,

@@ -47,13 +47,27 @@ def fdivstar(lam, u, p, dx):
     return lam * torch.sum((p * dx) * (torch.exp(u / lam) - 1))
 
 
+# Rows per block of the dense sums below: large problems are summed block by
+# block (the same terms in a different order), so that the temporaries of a
+# 60,000 x 60,000 problem stay a few GB.
+BLOCK_ROWS = 4096
+
+
+def _blocked_sum(fn, n_rows):
+    total = 0.0
+    for r0 in range(0, n_rows, BLOCK_ROWS):
+        total = total + fn(slice(r0, min(n_rows, r0 + BLOCK_ROWS)))
+    return total
+
+
 def primal(C, K, R, dx, dy, p, q, a, b, epsilon, lambda1, lambda2):
     """optimal_transport.py:45-53 (np.nan_to_num of log 0 -> the most negative double)."""
     torch = _torch()
     n_rows, n_cols = p.shape[0], q.shape[0]
     marg = fdiv(lambda1, R @ dy, p, dx) + fdiv(lambda2, R.T @ dx, q, dy)
-    ent = epsilon * torch.sum(R * torch.nan_to_num(torch.log(R)) - R + K)
-    return marg + (ent + torch.sum(R * C)) / (n_rows * n_cols)
+    ent = epsilon * _blocked_sum(lambda s: torch.sum(R[s] * torch.nan_to_num(torch.log(R[s])) - R[s] + K[s]),
+                                 n_rows)
+    return marg + (ent + _blocked_sum(lambda s: torch.sum(R[s] * C[s]), n_rows)) / (n_rows * n_cols)
 
 
 def dual(C, K, R, dx, dy, p, q, a, b, epsilon, lambda1, lambda2):
@@ -62,12 +76,27 @@ def dual(C, K, R, dx, dy, p, q, a, b, epsilon, lambda1, lambda2):
     n_rows, n_cols = p.shape[0], q.shape[0]
     return (- fdivstar(lambda1, - epsilon * torch.log(a), p, dx)
             - fdivstar(lambda2, - epsilon * torch.log(b), q, dy)
-            - epsilon * torch.sum(R - K) / (n_rows * n_cols))
+            - epsilon * _blocked_sum(lambda s: torch.sum(R[s] - K[s]), n_rows) / (n_rows * n_cols))
 
 
-def _stabilised_kernel(u, C, v, eps):
+def _stabilised_kernel(u, C, v, eps, out=None):
+    """exp((u_i - C_ij + v_j) / eps), built block by block (into ``out`` when given)."""
     torch = _torch()
-    return torch.exp((u[:, None] - C + v[None, :]) / eps)
+    K = torch.empty_like(C) if out is None else out
+    for r0 in range(0, C.shape[0], BLOCK_ROWS):
+        s = slice(r0, min(C.shape[0], r0 + BLOCK_ROWS))
+        torch.exp((u[s, None] - C[s] + v[None, :]) / eps, out=K[s])
+    return K
+
+
+def _scaled(K, a, b):
+    """(K.T * a).T * b, block by block."""
+    torch = _torch()
+    R = torch.empty_like(K)
+    for r0 in range(0, K.shape[0], BLOCK_ROWS):
+        s = slice(r0, min(K.shape[0], r0 + BLOCK_ROWS))
+        torch.mul(K[s] * a[s, None], b[None, :], out=R[s])
+    return R
 
 
 def optimal_transport_duality_gap(C, G, lambda1, lambda2, epsilon, batch_size, tolerance, tau,
@@ -91,16 +120,16 @@ def optimal_transport_duality_gap(C, G, lambda1, lambda2, epsilon, batch_size, t
     n_iter = 0
     n_absorb = 0
     gap = math.inf
-    R = None
+    R = K = K0 = None
     for stage in range(n_scalings + 1):
         gap = math.inf
         u = u + eps_i * torch.log(a)
         v = v + eps_i * torch.log(b)
         eps_i = eps_i / scale_factor
-        K0 = torch.exp(-C / eps_i)
+        K0 = _stabilised_kernel(torch.zeros_like(u), C, torch.zeros_like(v), eps_i, out=K0 if stage else None)
         alpha1 = lambda1 / (lambda1 + eps_i)
         alpha2 = lambda2 / (lambda2 + eps_i)
-        K = _stabilised_kernel(u, C, v, eps_i)
+        K = _stabilised_kernel(u, C, v, eps_i, out=K if stage else None)
         a = torch.ones(n_rows, dtype=torch.float64, device=dev)
         b = torch.ones(n_cols, dtype=torch.float64, device=dev)
         old_a, old_b = a, b
@@ -115,7 +144,7 @@ def optimal_transport_duality_gap(C, G, lambda1, lambda2, epsilon, batch_size, t
                 if max(float(a.abs().max()), float(b.abs().max())) > tau:
                     u = u + eps_i * torch.log(a)
                     v = v + eps_i * torch.log(b)
-                    K = _stabilised_kernel(u, C, v, eps_i)
+                    K = _stabilised_kernel(u, C, v, eps_i, out=K)
                     a = torch.ones(n_rows, dtype=torch.float64, device=dev)
                     b = torch.ones(n_cols, dtype=torch.float64, device=dev)
                     n_absorb += 1
@@ -127,7 +156,7 @@ def optimal_transport_duality_gap(C, G, lambda1, lambda2, epsilon, batch_size, t
             true_a = a * torch.exp(u / eps_i)
             true_b = b * torch.exp(v / eps_i)
             if final:
-                R = (K.T * a).T * b
+                R = _scaled(K, a, b)
                 pri = primal(C, K0, R, dx, dy, p, q, true_a, true_b, eps_i, lambda1, lambda2)
                 dua = dual(C, K0, R, dx, dy, p, q, true_a, true_b, eps_i, lambda1, lambda2)
                 gap = float((pri - dua) / abs(pri))
@@ -140,7 +169,9 @@ def optimal_transport_duality_gap(C, G, lambda1, lambda2, epsilon, batch_size, t
         stats.update(iterations=n_iter, absorptions=n_absorb, gap=gap, max_iter=False)
     if math.isnan(gap):
         raise RuntimeError("Overflow encountered in duality gap computation, please report this incident")
-    return (K.T * a).T * b / C.shape[1]
+    R = _scaled(K, a, b)
+    del K, K0
+    return R.div_(C.shape[1])
 
 
 def default_cost(a, b):
@@ -159,7 +190,33 @@ def default_cost(a, b):
     n = flat.numel()
     k = n // 2
     if n % 2:
-        med = torch.kthvalue(flat, k + 1).values
+        med = kth_smallest(flat, k + 1)
     else:
-        med = 0.5 * (torch.kthvalue(flat, k).values + torch.kthvalue(flat, k + 1).values)
-    return C / med
+        med = 0.5 * (kth_smallest(flat, k) + kth_smallest(flat, k + 1))
+    return C.div_(med)
+
+
+def kth_smallest(flat, k, block=1 << 26):
+    """The k-th smallest (1-based) entry of a 1-D tensor, exactly (np.median's
+    middle values): bounds from a sorted sample, a blockwise count below and
+    between them, and a sort of only the entries between them."""
+    torch = _torch()
+    n = flat.numel()
+    if n <= block:
+        return float(torch.kthvalue(flat, k).values)
+    g = torch.Generator(device=flat.device).manual_seed(0)
+    sample = torch.sort(flat[torch.randint(0, n, (1 << 20,), device=flat.device, generator=g)]).values
+    q = k / n
+    for width in (0.002, 0.02, 0.2, 1.0):
+        lo = float(sample[max(0, int((q - width) * sample.numel()))]) if q - width > 0 else -math.inf
+        hi = float(sample[min(sample.numel() - 1, int((q + width) * sample.numel()))]) if q + width < 1 else math.inf
+        below = 0
+        mid = []
+        for b0 in range(0, n, block):
+            x = flat[b0:b0 + block]
+            below += int((x < lo).sum())
+            mid.append(x[(x >= lo) & (x <= hi)])
+        mid = torch.cat(mid)
+        if below < k <= below + mid.numel():
+            return float(torch.sort(mid).values[k - below - 1])
+    raise RuntimeError('kth_smallest: no bracket found')

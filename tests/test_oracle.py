@@ -164,3 +164,6 @@ def test_torch_fp64_restatement_matches_numpy_oracle(pair_golden):
     for (x, y) in ((a, b), (a[:40], b)):   # odd and even entry counts of the median
         np.testing.assert_allclose(tot.default_cost(torch.as_tensor(x), torch.as_tensor(y)).numpy(),
                                    oom.compute_default_cost_matrix(x, y), rtol=1e-13, atol=1e-13)
+    v = torch.as_tensor(rng.normal(size=200001))            # the blockwise selection of large tensors
+    for k in (1, 100000, 100001, 200001):
+        assert tot.kth_smallest(v, k, block=1 << 12) == float(torch.kthvalue(v, k).values)
