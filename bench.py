@@ -146,11 +146,12 @@ def coords_on_device(X, day):
     return (x0 * s).float().contiguous(), (x1 * s).float().contiguous()
 
 
-def cpu_sample(a, b, G, I_s, J_s, rng, stages=None):
+def cpu_sample(a, b, G, I_s, J_s, rng, stages=None, cfg=None):
     """Oracle (FP64 NumPy restatement) on a random cell subsample; returns
     (seconds, iterations, coupling, (a_s, b_s, G_s)). With ``stages`` (a dict),
     also the split of those seconds into cost and solve, and the subsampled
-    rows ('rows': (ri, rj))."""
+    rows ('rows': (ri, rj)). ``cfg`` replaces the benchmark's solver
+    parameters."""
     from oracle import ot_model as oom, optimal_transport as oot
     ri = np.sort(rng.choice(a.shape[0], I_s, replace=False))
     rj = np.sort(rng.choice(b.shape[0], J_s, replace=False))
@@ -169,7 +170,7 @@ def cpu_sample(a, b, G, I_s, J_s, rng, stages=None):
         return out
 
     t1 = time.perf_counter()
-    T, _ = oot.compute_transport_matrix(solver=counting, C=C, G=G_s.copy(), **CFG)
+    T, _ = oot.compute_transport_matrix(solver=counting, C=C, G=G_s.copy(), **(CFG if cfg is None else cfg))
     if stages is not None:
         stages['solve'] = time.perf_counter() - t1
     return time.perf_counter() - t0, iters[0], T, (a_s, b_s, G_s)
@@ -225,6 +226,12 @@ def blas_threads():
     return os.cpu_count() or 1
 
 
+# The oracle's whole 20000 x 25000 solve, timed once on the GPU host's 16 cores with growth_iters = 1
+# (oracle/fullsize_c1.py; profiles/cpu_oracle_fullsize_20000x25000.md): too long for a bench step.
+CPU_FULL_SIZE = {'growth_iters': 1, 'iterations': 450, 'cost_s': 5.83, 'solve_s': 250.6, 'total_s': 256.4,
+                 'cores': 16, 'per_iteration_vs_sample_extrapolation': 1.38}
+
+
 def run_reference(args):
     """Reference arm: the reference's CPU algorithm (the oracle port; the
     reference itself is not available on the GPU host) on bounded samples of
@@ -247,8 +254,10 @@ def run_reference(args):
     t_step = float(np.mean(times))
     it_s = float(np.mean(its))
     scale = (I_FULL * J_FULL) / (I_s * J_s)
-    # maps/s at full size from the sample's time scaled by I*J (the whole-pair oracle solve on the
-    # GPU host's cores took 0.9-1.1x of this extrapolation: profiles/cpu_oracle_fullsize_20000x25000.md)
+    # maps/s at full size from the sample's time scaled by I*J. The oracle's whole-pair solve, timed
+    # once on the same host's 16 cores, spent 1.38x more time per Sinkhorn iteration than this
+    # extrapolation assumes (its iterates no longer fit the caches): the value is an upper bound on
+    # the CPU's throughput (profiles/cpu_oracle_fullsize_20000x25000.md).
     value = 1.0 / (t_step * scale)
     sample = ('%dx%d random cell subsample of the 20000x25000 pair per step (own median), full FP64 oracle '
               'duality-gap solve x3 growth iterations (%.0f iterations); ms_per_step is the measured time of '
@@ -259,6 +268,7 @@ def run_reference(args):
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
             'config': {'workload': WORKLOAD, 'I': I_FULL, 'J': J_FULL, 'd': PCA_D},
             'sinkhorn_iter_per_s': it_s / t_step * (I_s * J_s) / (I_FULL * J_FULL),
+            'cpu_full_size_measured': CPU_FULL_SIZE,
             'cpu_baseline': {'value': value, 'unit': 'maps/s', 'cores': blas_threads(), 'kind': 'port',
                              'sample': sample},
             'e2e': {'value': value, 'unit': 'maps/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
@@ -415,7 +425,7 @@ def run_course(args, days_data):
     torch.cuda.synchronize()
     t_sub_batched = time.perf_counter() - t0
     t_plain = {}
-    for form in ('auto', 'materialized'):
+    for form in ('auto', 'materialized', 'onthefly'):
         D.solve(sub_pairs[0].cost, sub_pairs[0].G, sub_items[0][1], 0, want_tmap=False, want_potentials=True,
                 form=form)
         torch.cuda.synchronize()
@@ -462,13 +472,13 @@ def run_course(args, days_data):
             'batched_vs_plain': {
                 'subset_pairs': subset, 'subset_items': len(sub_items),
                 'batched_s': t_sub_batched, 'plain_auto_s': t_plain['auto'],
-                'plain_materialized_s': t_plain['materialized'],
+                'plain_materialized_s': t_plain['materialized'], 'plain_onthefly_s': t_plain['onthefly'],
                 'ratio_vs_best_plain': best_plain / t_sub_batched,
                 'plain_maps_per_s_extrapolated': len(items) / (best_plain * w_all / w_sub),
                 'ratio_full_extrapolated': (best_plain * w_all / w_sub) / t,
-                'note': 'plain = wotg_compute_transport_matrix per item (potentials out), the faster of the '
-                        'on-the-fly and materialised forms; full-course plain time extrapolated from the subset '
-                        'by sum(iterations * I * J)'},
+                'note': 'plain = wotg_compute_transport_matrix per item (potentials out), the fastest of the '
+                        'auto, on-the-fly and materialised forms over the subset; full-course plain time '
+                        'extrapolated from the subset by sum(iterations * I * J)'},
             'gpu_launches': int(launches), 'clocks': clk.summary(), 'peaks': {'kind': peak_kind},
             'roofline': roofline}
     if not args.no_cpu:

@@ -77,7 +77,8 @@ __device__ __forceinline__ void warp_lse_f64(float& m, double& S) {
     const float m2 = __shfl_xor_sync(0xffffffffu, m, o);
     const double S2 = __shfl_xor_sync(0xffffffffu, S, o);
     const float mn = fmaxf(m, m2);
-    S = S * exp2((double)(m - mn)) + S2 * exp2((double)(m2 - mn));
+    // the scale factors by the FP32 ex2 (2 ulp), the sums themselves in FP64
+    S = S * (double)ex2(m - mn) + S2 * (double)ex2(m2 - mn);
     m = mn;
   }
 }

@@ -681,7 +681,7 @@ __global__ void pop_finish_kernel(int64_t n, int nq, int ctas, int nparts, const
     for (int64_t cc = c_lo; cc <= c_hi; ++cc)
       for (int q = 0; q < nparts; ++q) {
         const int64_t slot = ((cc + t) * 128 + (i & 127)) * nparts + q;
-        S += (double)psum[slot * npop_max + kk] * exp2((double)(part[slot].x - M));
+        S += (double)psum[slot * npop_max + kk] * (double)ex2(part[slot].x - M);
       }
     out[(int64_t)(k0 + kk) * n + i] = S > 0.0 ? exp(base + log(S)) : 0.0;
   }

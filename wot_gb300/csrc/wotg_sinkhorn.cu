@@ -344,13 +344,17 @@ __global__ void col_combine_kernel(Geom g, Vecs V, Coef c, int parity) {
     const float o = PREC ? col_offset(V, g, j) : 0.f;
     double L;
     if (PREC) {
-      // the row-block partials merged in FP64 against their largest exponent
+      // the row-block partials merged in one pass, the sum in FP64 against the
+      // running maximum (FP32 scale factors, 2 ulp)
       float m = kNegBig;
-      for (int r = 0; r < g.nrb; ++r) m = fmaxf(m, V.part[(int64_t)r * g.ldc + j].x);
       double S = 0.0;
       for (int r = 0; r < g.nrb; ++r) {
         const float2 ps = V.part[(int64_t)r * g.ldc + j];
-        S += (double)ps.y * exp2((double)(ps.x - m));
+        if (ps.x > m) {
+          S *= (double)ex2(m - ps.x);
+          m = ps.x;
+        }
+        S += (double)ps.y * (double)ex2(ps.x - m);
       }
       L = ((double)o + (double)m + log2(S)) * kLn2;
     } else {
