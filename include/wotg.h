@@ -422,6 +422,13 @@ int wotg_ot_adjoint(const float* X, int64_t I, int64_t ldx, const float* Y, int6
  * element, so this is their ceiling; allocates nothing; synchronises the stream. */
 int wotg_exp2_rate(double* exp2_per_s, void* stream);
 
+/* Diagnostic (no counterpart in the reference): out[i] = 2^z[i] (n FP32 values
+ * on the device) by the FMA-pipe exponential that the tensor-core epilogue
+ * uses for a share of its elements (range reduction to [-1/2, 1/2], a degree-5
+ * minimax polynomial, the exponent bits; z clamped to [-125, 126], NaN kept).
+ * Lets a test hold it to its error bound against FP64 2^z. Asynchronous. */
+int wotg_exp2_fma(const float* z, float* out, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -210,3 +210,31 @@ def test_bounded_wait_runs_out_and_the_device_recovers():
     a = D.solve(cost, g, DEFAULTS, 0, form='materialized')
     b = D.solve(cost, g, DEFAULTS, 0, form='onthefly')
     assert_parity(b.tmap.cpu().numpy(), a.tmap.cpu().numpy(), marginals=False)
+
+
+def test_fma_pipe_exp2_meets_its_bound():
+    """The FMA-pipe 2^z of the epilogue (range reduction, degree-5 minimax
+    polynomial, exponent bits) against FP64 2^z: relative error <= 3e-7 on
+    [-125, 126] (the polynomial's 7.5e-8 plus FP32 Horner rounding); beyond the
+    clamp, 2^126 (far above the speculative form's safe range, so such a row is
+    recomputed exactly) and at most 2^-125; NaN stays NaN."""
+    import torch
+    from wot_gb300 import _native as N
+    lib = N.load()
+    z = np.concatenate([np.linspace(-125, 126, 2_000_003), np.linspace(-0.5, 0.5, 100_001),
+                        [-np.inf, -1e30, -200.0, -125.5, 126.5, 300.0, 1e30, np.inf, np.nan]]).astype(np.float32)
+    zt = torch.as_tensor(z, device='cuda')
+    out = torch.empty_like(zt)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.wotg_exp2_fma(zt.data_ptr(), out.data_ptr(), z.size, st) == 0
+    r = out.cpu().numpy().astype(np.float64)
+    zd = z.astype(np.float64)
+    inside = (zd >= -125) & (zd <= 126)
+    ref = np.exp2(zd[inside])
+    assert (np.abs(r[inside] - ref) / ref).max() <= 3e-7
+    above = zd > 126
+    assert np.all(r[above] >= 2.0 ** 126 * (1 - 3e-7))
+    below = zd < -125
+    assert np.all((r[below] >= 0) & (r[below] <= 2.0 ** -125 * (1 + 3e-7)))
+    assert np.isnan(r[np.isnan(zd)]).all()
+    assert lib.wotg_exp2_fma(zt.data_ptr(), out.data_ptr(), 0, st) == N.WOTG_BADARG

@@ -208,15 +208,6 @@ __device__ __forceinline__ double item_b_update(Item& it, int64_t j, double L) {
   return lb_new;
 }
 
-// L2 = o + log2(s) for a sum s = m 2^e: the exponent exactly, the FP32 log2 of
-// the mantissa (absolute error ~1e-7, below the FP32 sum's own rounding), no
-// FP64 transcendental.
-__device__ __forceinline__ double lse2(float o, float s) {
-  int e;
-  const float m = frexpf(s, &e);
-  return (double)o + (double)e + (double)log2f(m);
-}
-
 // L2 = base-2 log-sum-exp of row r for entry e; returns the log-scaling whose
 // maximum over rows feeds the absorption test (log a_i or log b_j), else -inf.
 __device__ __forceinline__ double entry_epilogue(Item* items, const Entry& e, int64_t r, double L2) {

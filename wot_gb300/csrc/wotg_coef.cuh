@@ -16,6 +16,10 @@ struct Coef {
   double kappa;             // cost_scale / eps
   float kappa2;             // cost_scale / eps * log2(e), rounded towards zero
   float kappa2_lo;          // the remainder (> 0), so kappa2 + kappa2_lo carries ~48 bits
+  // log(tau) -/+ 1e-9: the absorption test max exp(la) > tau is decided from la
+  // alone outside this band (set by the single-problem driver; by default the
+  // band is the whole line, i.e. exp is always formed)
+  double ltau_lo, ltau_hi;
 };
 
 // The reference's exponents alpha1 = lambda1 / (lambda1 + eps) and
@@ -47,6 +51,8 @@ __host__ __device__ inline Coef make_coef(double eps, double lambda1, double lam
   if (!(lo > 0.f)) lo = 1e-30f;
   c.kappa2 = hi;
   c.kappa2_lo = lo;
+  c.ltau_lo = -INFINITY;
+  c.ltau_hi = INFINITY;
   return c;
 }
 

@@ -49,6 +49,51 @@ __device__ __forceinline__ float ex2(float x) {
   return y;
 }
 
+// 2^z of a pair on the FMA pipe (the tensor-core epilogue computes a share of
+// its exponentials here, beside the SFU): Cody-Waite style reduction
+// z = n + f with n = rint(z) (the 1.5 * 2^23 shift), f in [-1/2, 1/2]; 2^f by
+// the degree-5 relative-error minimax polynomial on [-1/2, 1/2] (Remez
+// exchange, max 7.5e-8; its FP32 Horner evaluation 2.2e-7 of 2^z); 2^n from
+// the exponent bits. z is clamped to [-125, 126] with NaN kept, so 2^n stays a
+// normal number and a NaN exponent gives NaN.
+__device__ __forceinline__ float2 ex2_fma2(float2 z) {
+  float zx, zy;
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(zx) : "f"(z.x), "f"(126.f));
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(zy) : "f"(z.y), "f"(126.f));
+  asm("max.NaN.f32 %0, %1, %2;" : "=f"(zx) : "f"(zx), "f"(-125.f));
+  asm("max.NaN.f32 %0, %1, %2;" : "=f"(zy) : "f"(zy), "f"(-125.f));
+  const float2 zz = make_float2(zx, zy);
+  const float2 t = __fadd2_rn(zz, make_float2(12582912.f, 12582912.f));        // 1.5 * 2^23 + n
+  const float2 n = __fadd2_rn(t, make_float2(-12582912.f, -12582912.f));
+  const float2 f = __fadd2_rn(zz, make_float2(-n.x, -n.y));                     // exact
+  float2 p = make_float2(1.3276472e-3f, 1.3276472e-3f);
+  p = __ffma2_rn(p, f, make_float2(9.675541e-3f, 9.675541e-3f));
+  p = __ffma2_rn(p, f, make_float2(5.550713e-2f, 5.550713e-2f));
+  p = __ffma2_rn(p, f, make_float2(0.2402212f, 0.2402212f));
+  p = __ffma2_rn(p, f, make_float2(0.69314694f, 0.69314694f));
+  p = __ffma2_rn(p, f, make_float2(1.0000001f, 1.0000001f));
+  // low bits of t hold n (two's complement): (t << 23) + (127 << 23) = the bits of 2^n
+  const float2 sc = make_float2(__int_as_float((__float_as_int(t.x) << 23) + (127 << 23)),
+                                __int_as_float((__float_as_int(t.y) << 23) + (127 << 23)));
+  return __fmul2_rn(p, sc);
+}
+
+// L2 = o + log2(s) for an FP32 sum s = m 2^e: the exponent exactly, the FP32
+// log2 of the mantissa taken in [1/sqrt 2, sqrt 2), so that for s near 1 (the
+// speculative half-steps, whose sums are relative to the previous log-sum-exp)
+// log2 m is small and its 1-ulp error negligible, and at most 3e-8 elsewhere
+// (below the FP32 sum's own rounding); no FP64 transcendental (slow on this
+// part). s = 0 gives -inf.
+__device__ __forceinline__ double lse2(float o, float s) {
+  int e;
+  float m = frexpf(s, &e);
+  if (m < 0.70710678f) {
+    m *= 2.f;
+    e -= 1;
+  }
+  return (double)o + (double)e + (double)log2f(m);
+}
+
 // Streaming 128-bit load that is not kept in L1 (each cost element is read
 // once per pass; the matrix is far larger than L2).
 __device__ __forceinline__ float4 ld_stream(const float4* p) { return __ldcs(p); }

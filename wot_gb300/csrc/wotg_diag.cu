@@ -58,3 +58,30 @@ extern "C" int wotg_exp2_rate(double* exp2_per_s, void* stream) {
   *exp2_per_s = (double)blocks * 256.0 * n * 4.0 / (best * 1e-3);
   return WOTG_OK;
 }
+
+namespace wotg {
+namespace {
+
+__global__ void exp2_fma_kernel(const float* __restrict__ z, float* __restrict__ out, int64_t n) {
+  const int64_t i = 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  if (i + 1 < n) {
+    const float2 r = ex2_fma2(make_float2(z[i], z[i + 1]));
+    out[i] = r.x;
+    out[i + 1] = r.y;
+  } else if (i < n) {
+    out[i] = ex2_fma2(make_float2(z[i], 0.f)).x;
+  }
+}
+
+}  // namespace
+}  // namespace wotg
+
+extern "C" int wotg_exp2_fma(const float* z, float* out, int64_t n, void* stream) {
+  if (!z || !out || n <= 0) return WOTG_BADARG;
+  const int64_t pairs = (n + 1) / 2;
+  const int64_t blocks = (pairs + 255) / 256;
+  if (blocks > 2147483647LL) return WOTG_BADARG;
+  wotg::exp2_fma_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(z, out, n);
+  WOTG_LAUNCHED();
+  return WOTG_OK;
+}

@@ -100,7 +100,10 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const float* __restric
 //   row form     a = [gamma x_1 .. gamma x_d, 1, 1, 0 ...]   (repacked per epsilon)
 //   column form  b = [x_1 .. x_d, beta1_q, beta2_q, 0 ...]   (bias columns per half-step)
 // where beta1 + beta2 carries the FP64 bias to ~44 bits (beta1 = fp32(bias),
-// beta2 = the remainder after beta1's hi/lo split). Points beyond n are zero.
+// beta2 = the remainder after beta1's hi/lo split). Points beyond n are zero,
+// and in the column form carry the bias of weight 0 (beta1 = -60000) from the
+// start: the bias columns of real points are rewritten per half-step, those of
+// the padding never.
 // ---------------------------------------------------------------------------
 __global__ void tc_pack_kernel(const float* __restrict__ X, int64_t n, int64_t ldx, int d, int kp, float scale,
                                int row_form, __half* __restrict__ tiles, double* __restrict__ norm) {
@@ -114,6 +117,7 @@ __global__ void tc_pack_kernel(const float* __restrict__ X, int64_t n, int64_t l
     float x = 0.f;
     if (k < d) x = i < n ? scale * X[i * ldx + k] : 0.f;
     else if (row_form && k < d + 2) x = 1.f;
+    else if (!row_form && i >= n && k == d) x = -60000.f;
     __half h, l;
     tc::split_f16(x, h, l);
     __half* tile = tiles + (i / 128) * tile_halfs;
@@ -140,30 +144,9 @@ __global__ void tc_pack_kernel(const float* __restrict__ X, int64_t n, int64_t l
 __global__ void tc_bias_pack_kernel(int64_t n, int64_t n_pad, const double* __restrict__ pot,
                                     const double* __restrict__ lsc, const double* __restrict__ norm,
                                     double inv_eps, double kappa2d, int d, int kp, __half* __restrict__ tiles) {
-  const int64_t tile_halfs = (int64_t)2 * 128 * kp;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += (int64_t)gridDim.x * blockDim.x) {
-    __half h1, l1, h2, l2;
-    const __half zero = __float2half_rn(0.f);
-    double beta = i < n ? (pot[i] * inv_eps + (lsc ? lsc[i] : 0.0)) * kLog2e - kappa2d * norm[i] : -INFINITY;
-    if (beta != beta || beta == INFINITY) {
-      h1 = __float2half_rn(NAN);
-      l1 = h2 = l2 = zero;
-    } else if (beta < -60000.0) {
-      h1 = __float2half_rn(-60000.f);
-      l1 = h2 = l2 = zero;
-    } else {
-      const float b1 = (float)beta;
-      tc::split_f16(b1, h1, l1);
-      const float b2 = (float)(beta - (double)__half2float(h1) - (double)__half2float(l1));
-      tc::split_f16(b2, h2, l2);
-    }
-    __half* tile = tiles + (i / 128) * tile_halfs;
-    const uint32_t o1 = tc::core_offset((int)(i % 128), d, kp) >> 1;
-    const uint32_t o2 = tc::core_offset((int)(i % 128), d + 1, kp) >> 1;
-    tile[o1] = h1;
-    tile[o2] = h2;
-    tile[128 * kp + o1] = l1;
-    tile[128 * kp + o2] = l2;
+    const double beta = i < n ? (pot[i] * inv_eps + (lsc ? lsc[i] : 0.0)) * kLog2e - kappa2d * norm[i] : -INFINITY;
+    tc_write_bias(i, beta, d, kp, tiles);
   }
 }
 
@@ -276,21 +259,21 @@ __device__ __forceinline__ void lse32(const float (&d)[32], float& m, float& s) 
   m = mn;
 }
 
-// Sum of 2^(d[c] - o) of 32 exponents into s (speculative form: o is the row's
-// log-sum-exp from the previous half-step, so no running maximum is needed).
-__device__ __forceinline__ void sum32_off(const float (&d)[32], float o, float& s) {
+// Sums of 2^(d[c] - o) of 32 exponents into four FP32x2 accumulators
+// (speculative form: o is the row's log-sum-exp from the previous half-step, so
+// no running maximum is needed). kFmaPairs of the 16 pairs take their 2^z on
+// the FMA pipe (ex2_fma2), the rest on the SFU: the epilogue's SFU, TMEM-load
+// and tensor work then overlap better (4 of 32 measured best; more moves the
+// bound to instruction issue).
+constexpr int kFmaPairs = 2;
+__device__ __forceinline__ void sum32_off(const float (&d)[32], float o, float2 (&acc)[4]) {
   const float2 neg = make_float2(-o, -o);
-  float2 e[16];
 #pragma unroll
   for (int c = 0; c < 16; ++c) {
     const float2 z = __fadd2_rn(make_float2(d[2 * c], d[2 * c + 1]), neg);
-    e[c] = make_float2(ex2(z.x), ex2(z.y));
+    const float2 e = c < kFmaPairs ? ex2_fma2(z) : make_float2(ex2(z.x), ex2(z.y));
+    acc[c & 3] = __fadd2_rn(acc[c & 3], e);
   }
-#pragma unroll
-  for (int w = 8; w >= 1; w >>= 1)
-#pragma unroll
-    for (int c = 0; c < w; ++c) e[c] = __fadd2_rn(e[c], e[c + w]);
-  s += e[0].x + e[0].y;
 }
 
 // Weighted sums of 32 exponents for up to NPOP populations at once (the
@@ -506,6 +489,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
     const int wq = warp & 3, cq = (warp - 2) >> 2;
     const int row = 32 * wq + lane;
     float m = kNegBig, s = 0.f;
+    float2 acc[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
     float sp[NPOP > 0 ? NPOP : 1];
 #pragma unroll
     for (int k = 0; k < (NPOP > 0 ? NPOP : 1); ++k) sp[k] = 0.f;
@@ -527,31 +511,49 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
       static_assert(kTcColsPerWarp == 64, "two 32-column TMEM blocks per warp and tile");
       const uint32_t taddr = tmem + ((uint32_t)(32 * wq) << 16) + (uint32_t)(128 * b + kTcColsPerWarp * cq);
       float d0[32], d1[32];
-      // first block, then the second block's load runs under the first block's sums
-      tc::tmem_ld32(taddr, d0);
-      tc::tmem_wait_ld();
-      tc::tmem_hold(d0);
-      tc::tmem_ld32(taddr + 32, d1);
       const int col0 = q * 128 + kTcColsPerWarp * cq;   // first column of d0 within the column set
-      if constexpr (NPOP > 0)
+      if constexpr (NPOP > 0) {
+        // first block, then the second block's load runs under the first
+        // block's sums (fewer live registers beside the population sums)
+        tc::tmem_ld32(taddr, d0);
+        tc::tmem_wait_ld();
+        tc::tmem_hold(d0);
+        tc::tmem_ld32(taddr + 32, d1);
         multi32<NPOP>(d0, popw, npop, ldpw, col0, m, sp);
-      else if (off)
-        sum32_off(d0, m, s);
-      else
-        lse32(d0, m, s);
-      tc::tmem_wait_ld();
-      tc::tmem_hold(d1);
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
-      if constexpr (NPOP > 0)
+        tc::tmem_wait_ld();
+        tc::tmem_hold(d1);
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
         multi32<NPOP>(d1, popw, npop, ldpw, col0 + 32, m, sp);
-      else if (off)
-        sum32_off(d1, m, s);
-      else
-        lse32(d1, m, s);
+      } else {
+        // both 32-column blocks loaded at once and the accumulator handed back
+        // to the MMA issuer before any sums (measured 3 % faster than
+        // overlapping the second load with the first block's sums)
+        tc::tmem_ld32(taddr, d0);
+        tc::tmem_ld32(taddr + 32, d1);
+        tc::tmem_wait_ld();
+        tc::tmem_hold(d0);
+        tc::tmem_hold(d1);
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+        if (off) {
+          sum32_off(d0, m, acc);
+          sum32_off(d1, m, acc);
+        } else {
+          lse32(d0, m, s);
+          lse32(d1, m, s);
+        }
+      }
       if (++q == nq || j == n - 1) {
         const int64_t slot = (((int64_t)blockIdx.x + t) * 128 + row) * kTcParts + cq;
+        if (NPOP == 0 && off) {
+          const float2 a = __fadd2_rn(__fadd2_rn(acc[0], acc[1]), __fadd2_rn(acc[2], acc[3]));
+          s = a.x + a.y;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) acc[k] = make_float2(0.f, 0.f);
+        }
         part[slot] = make_float2(m, s);
         if constexpr (NPOP > 0) {
 #pragma unroll
@@ -641,7 +643,7 @@ __global__ void lse_points_finish_kernel(int64_t n, int nq, int ctas, int nparts
     const float2* pp = part + ((cc + t) * 128 + (i & 127)) * nparts;
     for (int k = 0; k < nparts; ++k) lse_merge(m, s, pp[k].x, pp[k].y);
   }
-  const double D = (double)m + log2((double)s);
+  const double D = lse2(m, s);
   if (L) L[i] = D * kLn2 - scale * norm[i];
   if (off) off[i] = (float)D;
 }

@@ -87,12 +87,18 @@ struct TcState {
   // Speculative half-steps: each row's base-2 log-sum-exp of the MMA exponents
   // from the previous half-step (row side offX, column side offY), valid while
   // epsilon is unchanged; rows whose sum left the safe range are listed in
-  // redo = [count, rows...] and recomputed exactly.
+  // redoX / redoY = [count, rows...] (row and column passes) and recomputed
+  // exactly; each side's combine empties the other side's list.
   float* offX;
   float* offY;
-  int* redo;
+  int* redoX;
+  int* redoY;
   unsigned long long* redo_total;  // rows recomputed exactly, over the solve (diagnostic)
   bool off_row_ok, off_col_ok;
+  // Column-form biases of X (read by column passes) and Y (row passes) match
+  // the current potentials: written by the combine of the half-step that
+  // updated them, else packed before the pass that reads them.
+  bool xb_ok, yb_ok;
 };
 
 struct Geom {
@@ -104,6 +110,16 @@ struct Geom {
 
 // The reference's a-update for row i; returns the new a_i (for the
 // absorption test, reduced per block by the caller).
+// exp(la) as the absorption test needs it: the test only compares the largest
+// exp(la) with tau, so away from log(tau) the value is 0 (below) or +inf
+// (above) with the same outcome, and the FP64 exp (slow on this part) is formed
+// only within 1e-9 of log(tau). NaN stays NaN.
+__device__ __forceinline__ double absorb_key(double la, const Coef& c) {
+  if (la < c.ltau_lo) return 0.0;
+  if (la > c.ltau_hi) return INFINITY;
+  return exp(la);
+}
+
 __device__ __forceinline__ double a_update(int64_t i, double L, const Vecs& V, const Coef& c) {
   const double ui = V.u[i];
   const double logs = ui * c.inv_eps + L - c.logJ;                 // log (K (b dy))_i
@@ -111,7 +127,7 @@ __device__ __forceinline__ double a_update(int64_t i, double L, const Vecs& V, c
   V.la_old[i] = V.la[i];
   V.la[i] = la_new;
   split_weight((ui * c.inv_eps + la_new) * kLog2e, V.wrow, V.wrow_lo, i);
-  return exp(la_new);
+  return absorb_key(la_new, c);
 }
 
 __device__ __forceinline__ double b_update(int64_t j, double L, const Vecs& V, const Coef& c) {
@@ -121,7 +137,7 @@ __device__ __forceinline__ double b_update(int64_t j, double L, const Vecs& V, c
   V.lb_old[j] = V.lb[j];
   V.lb[j] = lb_new;
   split_weight((vj * c.inv_eps + lb_new) * kLog2e, V.wcol, V.wcol_lo, j);
-  return exp(lb_new);
+  return absorb_key(lb_new, c);
 }
 
 // Block-wide max of the threads' values, folded into the absorption slot with
@@ -363,7 +379,7 @@ __global__ void col_combine_kernel(Geom g, Vecs V, Coef c, int parity) {
         const float2 ps = V.part[(int64_t)r * g.ldc + j];
         lse_merge(m, s, ps.x, ps.y);
       }
-      L = ((double)m + log2((double)s)) * kLn2;
+      L = lse2(m, s) * kLn2;
     }
     V.Lcol[j] = L;
     if (UPDATE_B) bmax = b_update(j, L, V, c);
@@ -373,23 +389,28 @@ __global__ void col_combine_kernel(Geom g, Vecs V, Coef c, int parity) {
 
 // tau-absorption (optimal_transport.py:137-141 / :211-216): if max(a, b) > tau,
 // u += eps log a, v += eps log b, a = b = 1. Also clears the other max slot.
-__global__ void absorb_kernel(Geom g, Vecs V, Coef c, double tau, int parity) {
+// The on-the-fly form also rewrites the column-form biases of the absorbed
+// points (bx, by; tiles = nullptr in the materialised form).
+__global__ void absorb_kernel(Geom g, Vecs V, Coef c, double tau, int parity, TcBias bx, TcBias by) {
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const double mx = __longlong_as_double((long long)V.maxslot[parity]);
   if (idx == 0) V.maxslot[parity ^ 1] = 0ull;
   if (!(mx > tau)) return;
   if (idx == 0) V.counters[0] += 1;
+  const double k2d = c.kappa * kLog2e;
   if (idx < g.I) {
     const double un = V.u[idx] + c.eps * V.la[idx];
     V.u[idx] = un;
     V.la[idx] = 0.0;
     split_weight(un * c.inv_eps * kLog2e, V.wrow, V.wrow_lo, idx);
+    if (bx.tiles) tc_write_bias(idx, (un * c.inv_eps + 0.0) * kLog2e - k2d * bx.norm[idx], bx.d, bx.kp, bx.tiles);
   } else if (idx < g.I + g.J) {
     const int64_t j = idx - g.I;
     const double vn = V.v[j] + c.eps * V.lb[j];
     V.v[j] = vn;
     V.lb[j] = 0.0;
     split_weight(vn * c.inv_eps * kLog2e, V.wcol, V.wcol_lo, j);
+    if (by.tiles) tc_write_bias(j, (vn * c.inv_eps + 0.0) * kLog2e - k2d * by.norm[j], by.d, by.kp, by.tiles);
   }
 }
 
@@ -654,12 +675,26 @@ __global__ void __launch_bounds__(256) coupling_kernel(const float* __restrict__
 // Merge of the tensor-core kernel's partials: one thread per point, over the
 // (CTA, column quarter) partials whose stretch covered the point's row tile
 // (FP32 LSE merge), then the FP64 finish and update.
+// Column-form bias of point i of the side a half-step just updated (ROW: a row
+// point with its new log-scaling la, for the next column pass; else a column
+// point with its new lb, for the next row pass).
+template <bool ROW>
+__device__ __forceinline__ void write_bias(int64_t i, const Vecs& V, const Coef& c, const TcBias& b) {
+  const double pot = ROW ? V.u[i] : V.v[i];
+  const double lsc = ROW ? V.la[i] : V.lb[i];
+  tc_write_bias(i, (pot * c.inv_eps + lsc) * kLog2e - (c.kappa * kLog2e) * b.norm[i], b.d, b.kp, b.tiles);
+}
+
 template <bool ROW, bool UPDATE>
 __global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restrict__ part, int nq, int ctas,
                                   int nparts, const double* __restrict__ norm, int parity, int spec,
-                                  float* __restrict__ off, int* __restrict__ redo) {
+                                  float* __restrict__ off, int* __restrict__ redo, int* __restrict__ redo_other,
+                                  TcBias bias) {
   const int64_t n = ROW ? g.I : g.J;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // the other side's list of exactly recomputed rows was consumed by its last
+  // half-step (earlier in the stream): empty it for that side's next one
+  if (i == 0) redo_other[0] = 0;
   double vmax = 0.0;
   bool skip = false;
   if (i < n) {
@@ -681,7 +716,7 @@ __global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restri
       redo[1 + k] = (int)i;
       skip = true;
     } else {
-      const double D = (double)m + log2((double)s);
+      const double D = lse2(m, s);
       off[i] = (float)D;
       const double L = D * kLn2 - c.kappa * norm[i];
       if (ROW) {
@@ -691,6 +726,7 @@ __global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restri
         V.Lcol[i] = L;
         if (UPDATE) vmax = b_update(i, L, V, c);
       }
+      if (UPDATE && bias.tiles) write_bias<ROW>(i, V, c, bias);
     }
   }
   (void)skip;
@@ -704,7 +740,7 @@ template <bool ROW, bool UPDATE>
 __global__ void tc_exact_rows_kernel(Geom g, Vecs V, Coef c, const float* __restrict__ P, int64_t ldp,
                                      const float* __restrict__ Q, int64_t ldq, int d, const double* __restrict__ norm,
                                      float* __restrict__ off, int* __restrict__ redo,
-                                     unsigned long long* __restrict__ total, int parity) {
+                                     unsigned long long* __restrict__ total, int parity, TcBias bias) {
   const int cnt = redo[0];
   if (blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0) atomicAdd(total, (unsigned long long)cnt);
   const int lane = threadIdx.x & 31;
@@ -730,7 +766,7 @@ __global__ void tc_exact_rows_kernel(Geom g, Vecs V, Coef c, const float* __rest
     }
     warp_lse(m, s);
     if (lane == 0) {
-      const double L2 = (double)m + log2((double)s);
+      const double L2 = lse2(m, s);
       off[i] = (float)(L2 + (double)k2 * norm[i]);
       const double L = L2 * kLn2;
       double v = 0.0;
@@ -742,6 +778,7 @@ __global__ void tc_exact_rows_kernel(Geom g, Vecs V, Coef c, const float* __rest
         if (UPDATE) v = b_update(i, L, V, c);
       }
       if (UPDATE) atomic_max_nonneg(V.maxslot + parity, v);
+      if (UPDATE && bias.tiles) write_bias<ROW>(i, V, c, bias);
     }
   }
 }
@@ -759,7 +796,10 @@ struct Solver {
   TcState tc;
 
   Coef coef(double eps, const wotg_params& P, double q) const {
-    return make_coef(eps, P.lambda1, P.lambda2, cost_scale, g.I, g.J, q);
+    Coef c = make_coef(eps, P.lambda1, P.lambda2, cost_scale, g.I, g.J, q);
+    c.ltau_lo = std::log(P.tau) - 1e-9;
+    c.ltau_hi = std::log(P.tau) + 1e-9;
+    return c;
   }
 
   int vec_blocks(int64_t n) const { return (int)std::max<int64_t>(1, (n + 255) / 256); }
@@ -771,8 +811,11 @@ struct Solver {
   // (FP16 range); their product is gamma x . y.
   int tc_prepare(const Coef& c) {
     if (!tc.on) return WOTG_OK;
-    tc.off_row_ok = false;  // a new epsilon: the offsets of both sides are stale
+    tc.off_row_ok = false;  // a new epsilon: the offsets and biases of both sides are stale
     tc.off_col_ok = false;
+    tc.xb_ok = tc.yb_ok = false;
+    WOTG_CUDA(cudaMemsetAsync(tc.redoX, 0, sizeof(int), st));
+    WOTG_CUDA(cudaMemsetAsync(tc.redoY, 0, sizeof(int), st));
     const float gamma = (float)(2.0 * c.kappa * kLog2e / std::sqrt(cost_scale));
     int s = tc_pack_points(tc.X, g.I, tc.ldx, tc.d, tc.kp, gamma, 1, tc.Xa, nullptr, st);
     if (s) return s;
@@ -782,45 +825,57 @@ struct Solver {
   // The half-steps run in the speculative form once the offsets of their side
   // exist for the current epsilon (the first half-step of each side after an
   // epsilon change or a new solve runs the exact form and writes them).
+  TcBias bias_x() const { return TcBias{tc.Xb, tc.normX, tc.d, tc.kp}; }
+  TcBias bias_y() const { return TcBias{tc.Yb, tc.normY, tc.d, tc.kp}; }
+
   template <bool UPDATE>
   int tc_row_pass(const Coef& c, int parity) {
-    int s = tc_pack_bias(g.J, V.v, V.lb, tc.normY, c.inv_eps, c.kappa * kLog2e, tc.d, tc.kp, tc.Yb, st);
-    if (s) return s;
+    if (!tc.yb_ok) {
+      int s = tc_pack_bias(g.J, V.v, V.lb, tc.normY, c.inv_eps, c.kappa * kLog2e, tc.d, tc.kp, tc.Yb, st);
+      if (s) return s;
+      tc.yb_ok = true;
+    }
     const bool spec = tc.off_row_ok;
-    if (spec) WOTG_CUDA(cudaMemsetAsync(tc.redo, 0, sizeof(int), st));
-    s = tc_lse_launch(tc.Xa, tc.n_xt, tc.Yb, tc.n_yt, tc.kp, tc.ctas_row, tc.part, spec ? tc.offX : nullptr,
-                      tc.err, st);
+    int s = tc_lse_launch(tc.Xa, tc.n_xt, tc.Yb, tc.n_yt, tc.kp, tc.ctas_row, tc.part, spec ? tc.offX : nullptr,
+                          tc.err, st);
     if (s) return s;
+    const TcBias bx = UPDATE ? bias_x() : TcBias{};
     tc_combine_kernel<true, UPDATE><<<vec_blocks(g.I), 256, 0, st>>>(
-        g, V, c, tc.part, tc.n_yt, tc.ctas_row, tc_parts(), tc.normX, parity, spec ? 1 : 0, tc.offX, tc.redo);
+        g, V, c, tc.part, tc.n_yt, tc.ctas_row, tc_parts(), tc.normX, parity, spec ? 1 : 0, tc.offX, tc.redoX,
+        tc.redoY, bx);
     WOTG_LAUNCHED();
     if (spec) {
       tc_exact_rows_kernel<true, UPDATE><<<2 * sm_count(), 256, 0, st>>>(g, V, c, tc.X, tc.ldx, tc.Y, tc.ldy, tc.d,
-                                                                       tc.normX, tc.offX, tc.redo, tc.redo_total,
-                                                                       parity);
+                                                                       tc.normX, tc.offX, tc.redoX, tc.redo_total,
+                                                                       parity, bx);
       WOTG_LAUNCHED();
     }
     tc.off_row_ok = true;
+    if (UPDATE) tc.xb_ok = true;
     return WOTG_OK;
   }
   int tc_col_pass(const Coef& c, int parity) {
-    int s = tc_pack_bias(g.I, V.u, V.la, tc.normX, c.inv_eps, c.kappa * kLog2e, tc.d, tc.kp, tc.Xb, st);
-    if (s) return s;
+    if (!tc.xb_ok) {
+      int s = tc_pack_bias(g.I, V.u, V.la, tc.normX, c.inv_eps, c.kappa * kLog2e, tc.d, tc.kp, tc.Xb, st);
+      if (s) return s;
+      tc.xb_ok = true;
+    }
     const bool spec = tc.off_col_ok;
-    if (spec) WOTG_CUDA(cudaMemsetAsync(tc.redo, 0, sizeof(int), st));
-    s = tc_lse_launch(tc.Ya, tc.n_yt, tc.Xb, tc.n_xt, tc.kp, tc.ctas_col, tc.part, spec ? tc.offY : nullptr,
-                      tc.err, st);
+    int s = tc_lse_launch(tc.Ya, tc.n_yt, tc.Xb, tc.n_xt, tc.kp, tc.ctas_col, tc.part, spec ? tc.offY : nullptr,
+                          tc.err, st);
     if (s) return s;
     tc_combine_kernel<false, true><<<vec_blocks(g.J), 256, 0, st>>>(
-        g, V, c, tc.part, tc.n_xt, tc.ctas_col, tc_parts(), tc.normY, parity, spec ? 1 : 0, tc.offY, tc.redo);
+        g, V, c, tc.part, tc.n_xt, tc.ctas_col, tc_parts(), tc.normY, parity, spec ? 1 : 0, tc.offY, tc.redoY,
+        tc.redoX, bias_y());
     WOTG_LAUNCHED();
     if (spec) {
       tc_exact_rows_kernel<false, true><<<2 * sm_count(), 256, 0, st>>>(g, V, c, tc.Y, tc.ldy, tc.X, tc.ldx, tc.d,
-                                                                      tc.normY, tc.offY, tc.redo, tc.redo_total,
-                                                                      parity);
+                                                                      tc.normY, tc.offY, tc.redoY, tc.redo_total,
+                                                                      parity, bias_y());
       WOTG_LAUNCHED();
     }
     tc.off_col_ok = true;
+    tc.yb_ok = true;
     return WOTG_OK;
   }
 
@@ -831,6 +886,7 @@ struct Solver {
       if (lrow_valid) {
         a_update_kernel<<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, parity);
         WOTG_LAUNCHED();
+        tc.xb_ok = false;  // la changed without its biases: the column pass packs them
       } else {
         s = tc_row_pass<true>(c, parity);
         if (s) return s;
@@ -851,7 +907,8 @@ struct Solver {
   }
 
   int absorb(const Coef& c, double tau, int parity) {
-    absorb_kernel<<<vec_blocks(g.I + g.J), 256, 0, st>>>(g, V, c, tau, parity);
+    absorb_kernel<<<vec_blocks(g.I + g.J), 256, 0, st>>>(g, V, c, tau, parity, tc.on ? bias_x() : TcBias{},
+                                                         tc.on ? bias_y() : TcBias{});
     WOTG_LAUNCHED();
     return WOTG_OK;
   }
@@ -1189,9 +1246,11 @@ static void tc_layout(Bump& b, const wotg_problem* prob, TcState& tc) {
   tc.err = b.take<int>(4);
   tc.offX = b.take<float>(tc.I_pad);
   tc.offY = b.take<float>(tc.J_pad);
-  tc.redo = b.take<int>(2 + std::max(prob->I, prob->J));
+  tc.redoX = b.take<int>(2 + prob->I);
+  tc.redoY = b.take<int>(2 + prob->J);
   tc.redo_total = b.take<unsigned long long>(1);
   tc.off_row_ok = tc.off_col_ok = false;
+  tc.xb_ok = tc.yb_ok = false;
 }
 
 extern "C" size_t wotg_problem_workspace_bytes(const wotg_problem* prob) {
