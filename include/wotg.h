@@ -138,7 +138,11 @@ int wotg_median(const float* C, int64_t I, int64_t J, int64_t ldc, double* media
  *                   v + eps log b) of the last solve, so that
  *                   tmap = exp((u_bar_i + v_bar_j - cost_scale C_ij) / eps) / J
  *                   with eps = stats->final_epsilon.
- * stats (host) may be NULL. */
+ * stats (host) may be NULL. The final epsilon stage's batches of iterations
+ * between duality-gap checks run as CUDA graphs, captured once per stage on a
+ * stream of the call's own (ordered with `stream` by events; the stream, two
+ * events and at most two graphs live for the call); the no-alloc entry point
+ * launches plainly on `stream`. Results are the same either way. */
 size_t wotg_solve_workspace_bytes(int64_t I, int64_t J, int64_t ldc);   /* materialised form */
 size_t wotg_problem_workspace_bytes(const wotg_problem* problem);       /* any form */
 int wotg_compute_transport_matrix(const wotg_problem* problem, const wotg_params* params,

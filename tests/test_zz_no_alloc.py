@@ -90,8 +90,10 @@ def test_noalloc_matches_workspace_entry_point_on_consecutive_calls(pair_golden)
         st_a, ref, stats_a = _solve_both(lib, N, D, torch, C, G, cfg, solver, noalloc=False)
         st_b, got, stats_b = _solve_both(lib, N, D, torch, C, G, cfg, solver, noalloc=True)
         assert st_a == 0 and st_b == 0
+        # the workspace call replays the final stage's batches as CUDA graphs, the
+        # no-alloc call launches them plainly: the same kernels, the same results
         for k in ref:
-            assert _err(got[k], ref[k]) <= COUPLING_TOL, k
+            assert _err(got[k], ref[k]) <= 1e-12, k
         assert stats_b['iterations'] == stats_a['iterations']
         assert stats_b['exact_rows'] == stats_a['exact_rows']
     # and against the reference's own coupling for the golden pair

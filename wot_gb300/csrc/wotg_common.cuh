@@ -31,6 +31,9 @@ void set_last_message(const char* msg);
 
 // Host-side count of kernels this library launched (wotg_launch_count).
 void count_launch();
+// n kernels launched by one replay of a captured graph; the count so far.
+void count_launches(unsigned long long n);
+unsigned long long launches_so_far();
 
 #define WOTG_LAUNCHED()                                   \
   do {                                                    \

@@ -54,6 +54,7 @@ struct Vecs {
   float* wcol;     // ldc (v_j/eps + lb_j) * log2(e), zero in padding columns (hi part)
   float* wrow_lo;  // I   remainders of the weights (lo parts)
   float* wcol_lo;  // ldc
+  float4* rowc;    // I   per-row constants of the dense coupling (coupling_rows_kernel)
   float2* part;    // nrb x ldc column-pass partials (m, s) in base 2
   unsigned long long* maxslot;  // 2 slots of max(a, b) bits, alternating per iteration
   double* red;     // kRedBlocks x kNq reduction partials
@@ -360,16 +361,14 @@ __global__ void col_combine_kernel(Geom g, Vecs V, Coef c, int parity) {
     const float o = PREC ? col_offset(V, g, j) : 0.f;
     double L;
     if (PREC) {
-      // the row-block partials merged in one pass, the sum in FP64 against the
-      // running maximum (FP32 scale factors, 2 ulp)
+      // the row-block partials merged in FP64 against their largest exponent
+      // (FP32 scale factors, 2 ulp; two passes: measured faster than one pass
+      // with a running maximum, whose rescaling lengthens the FP64 chain)
       float m = kNegBig;
+      for (int r = 0; r < g.nrb; ++r) m = fmaxf(m, V.part[(int64_t)r * g.ldc + j].x);
       double S = 0.0;
       for (int r = 0; r < g.nrb; ++r) {
         const float2 ps = V.part[(int64_t)r * g.ldc + j];
-        if (ps.x > m) {
-          S *= (double)ex2(m - ps.x);
-          m = ps.x;
-        }
         S += (double)ps.y * (double)ex2(ps.x - m);
       }
       L = ((double)o + (double)m + log2(S)) * kLn2;
@@ -637,6 +636,28 @@ __global__ void potentials_kernel(Geom g, Vecs V, Coef c, double* __restrict__ u
   }
 }
 
+// Per-row constants of the dense coupling: the row's base-2 exponent
+//   t_ij = wr_i + wc_j - k2 C_ij,   wr_i = (u_i / eps + la_i + log_scale) log2 e,
+// is evaluated as t_ij = x_ij + E_i with x_ij = (wc_j - o_i) - k2 C_ij in FP32
+// (the streamed passes' split arithmetic, o_i the row's grid offset from its
+// log-sum-exp L_i, so x <= ~0 for the entries that carry mass) and
+// E_i = o_i + wr_i = n_i + f_i in FP64: rowc = (o_i, 2^f_i, n_i, 1); w = 0 marks
+// a row whose constants are not finite (its entries take the FP64 path).
+__global__ void coupling_rows_kernel(Geom g, Vecs V, Coef c, double log_scale) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.I) return;
+  const double wr = (V.u[i] * c.inv_eps + V.la[i] + log_scale) * kLog2e;
+  const double L = V.Lrow[i];
+  const float o = grid_offset(L);
+  const double E = (double)o + wr;
+  float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (fabs(L) < 1e30 && fabs(E) < 900.0) {
+    const double n = floor(E);
+    r = make_float4(o, (float)exp2(E - n), (float)n, 1.f);
+  }
+  V.rowc[i] = r;
+}
+
 // 2^t for an FP64 exponent t: the integer part exactly (as the FP64 exponent
 // field), the fraction by FP32 ex2 (relative error ~2^-22); 0 below 2^-1020,
 // NaN for NaN.
@@ -649,17 +670,41 @@ __device__ __forceinline__ double exp2_split(double t) {
 }
 
 // Dense coupling tmap_ij = a_i exp((u_i - C_ij + v_j)/eps) b_j * exp(log_scale), written
-// FP64 row-major (stride J) like the reference's ndarray. The exponent is formed in
-// FP64 (its terms are tens to hundreds; only the fraction goes through FP32).
+// FP64 row-major (stride J) like the reference's ndarray. 2^t_ij = (2^x_ij 2^f_i) 2^n_i
+// (coupling_rows_kernel): x_ij = fma(-k2hi, C, wc_hi - o_i) + fma(-k2lo, C, wc_lo) as in
+// the streamed passes (one FP32 rounding of a value that is small for the entries that
+// carry mass, below the FP32 storage of C), 2^x 2^f in FP32, and the power 2^n_i put into
+// the FP64 exponent field by integer arithmetic, so that no element needs FP64
+// arithmetic (slow on this part) and the kernel streams C in and the map out. Entries
+// whose 2^x or result leaves the normal ranges (far below a row's mass, or non-finite
+// inputs) take the FP64 exponent (exp2_split), which is exact in the same way.
 __global__ void __launch_bounds__(256) coupling_kernel(const float* __restrict__ C, Geom g, Vecs V,
                                                        Coef c, double log_scale, double* __restrict__ out) {
-  const double k2 = c.kappa * kLog2e;
   for (int64_t j0 = (int64_t)blockIdx.x * blockDim.x; j0 < g.J; j0 += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = j0 + threadIdx.x;
-    const double wc = j < g.J ? (V.v[j] * c.inv_eps + V.lb[j]) * kLog2e : 0.0;   // once per column
-    for (int64_t i = blockIdx.y; i < g.I && j < g.J; i += gridDim.y) {
-      const double wr = (V.u[i] * c.inv_eps + V.la[i] + log_scale) * kLog2e;
-      out[i * g.J + j] = exp2_split(wr + wc - k2 * (double)C[i * g.ldc + j]);
+    if (j >= g.J) continue;
+    const float hi = V.wcol[j], lo = V.wcol_lo[j];   // once per column
+    for (int64_t i = blockIdx.y; i < g.I; i += gridDim.y) {
+      const float4 rc = V.rowc[i];
+      const float cc = C[i * g.ldc + j];
+      const float x = fmaf(-c.kappa2, cc, hi - rc.x) + fmaf(-c.kappa2_lo, cc, lo);
+      double val;
+      bool done = false;
+      if (rc.w != 0.f && x > -125.f && x < 125.f) {
+        const float y = ex2(x) * rc.y;                              // normal, positive
+        const uint32_t yb = __float_as_uint(y);
+        const int e = (int)(yb >> 23) - 127 + (int)rc.z;           // exponent of the result
+        if (e > -1022 && e < 1023) {
+          val = __longlong_as_double((long long)((uint64_t)(e + 1023) << 52 | (uint64_t)(yb & 0x7FFFFFu) << 29));
+          done = true;
+        }
+      }
+      if (!done) {
+        const double wr = (V.u[i] * c.inv_eps + V.la[i] + log_scale) * kLog2e;
+        const double wc = (V.v[j] * c.inv_eps + V.lb[j]) * kLog2e;
+        val = exp2_split(wr + wc - c.kappa * kLog2e * (double)cc);
+      }
+      out[i * g.J + j] = val;
     }
   }
 }
@@ -674,7 +719,9 @@ __global__ void __launch_bounds__(256) coupling_kernel(const float* __restrict__
 // ---------------------------------------------------------------------------
 // Merge of the tensor-core kernel's partials: one thread per point, over the
 // (CTA, column quarter) partials whose stretch covered the point's row tile
-// (FP32 LSE merge), then the FP64 finish and update.
+// (FP32 LSE merge), then the FP64 finish and update. Launched in 64-thread
+// blocks: the per-row FP64 work is latency-bound, so spreading the rows over
+// every SM beats fewer, fuller blocks.
 // Column-form bias of point i of the side a half-step just updated (ROW: a row
 // point with its new log-scaling la, for the next column pass; else a column
 // point with its new lb, for the next row pass).
@@ -840,7 +887,7 @@ struct Solver {
                           tc.err, st);
     if (s) return s;
     const TcBias bx = UPDATE ? bias_x() : TcBias{};
-    tc_combine_kernel<true, UPDATE><<<vec_blocks(g.I), 256, 0, st>>>(
+    tc_combine_kernel<true, UPDATE><<<(unsigned)((g.I + 63) / 64), 64, 0, st>>>(
         g, V, c, tc.part, tc.n_yt, tc.ctas_row, tc_parts(), tc.normX, parity, spec ? 1 : 0, tc.offX, tc.redoX,
         tc.redoY, bx);
     WOTG_LAUNCHED();
@@ -864,7 +911,7 @@ struct Solver {
     int s = tc_lse_launch(tc.Ya, tc.n_yt, tc.Xb, tc.n_xt, tc.kp, tc.ctas_col, tc.part, spec ? tc.offY : nullptr,
                           tc.err, st);
     if (s) return s;
-    tc_combine_kernel<false, true><<<vec_blocks(g.J), 256, 0, st>>>(
+    tc_combine_kernel<false, true><<<(unsigned)((g.J + 63) / 64), 64, 0, st>>>(
         g, V, c, tc.part, tc.n_xt, tc.ctas_col, tc_parts(), tc.normY, parity, spec ? 1 : 0, tc.offY, tc.redoY,
         tc.redoX, bias_y());
     WOTG_LAUNCHED();
@@ -954,6 +1001,102 @@ struct Solver {
     return WOTG_OK;
   }
 
+  // CUDA-graph replay of the final stage's batches between duality-gap checks.
+  // In that stage a batch starts right after a check (L_row fresh) with both
+  // sides' speculative offsets and column-form biases current, and ends in the
+  // same host state, so its launches (nb iterations with their absorption
+  // tests, all arguments fixed for the stage) are captured once per starting
+  // parity and replayed; a new epsilon drops them.
+  struct BatchGraph {
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long launches = 0;
+    int nb = 0;
+  };
+  BatchGraph bg[2] = {};
+  cudaStream_t gs = nullptr;                 // private stream of the captures and replays
+  cudaEvent_t gev[2] = {nullptr, nullptr};
+  bool graphs_off = false;                   // no private stream: plain launches
+
+  bool steady() const { return !tc.on || (tc.off_row_ok && tc.off_col_ok && tc.xb_ok && tc.yb_ok); }
+
+  void drop_graphs() {
+    for (auto& b : bg) {
+      if (b.exec) cudaGraphExecDestroy(b.exec);
+      b = BatchGraph{};
+    }
+  }
+  void release_graphs() {
+    drop_graphs();
+    for (auto& e : gev)
+      if (e) cudaEventDestroy(e);
+    gev[0] = gev[1] = nullptr;
+    if (gs) cudaStreamDestroy(gs);
+    gs = nullptr;
+  }
+
+  // One batch of nb iterations from a fresh L_row at `parity`, as a graph;
+  // *used = false when graphs are unavailable (the caller launches plainly).
+  int batch_graph(const Coef& c, int nb, int parity, double tau, bool* used) {
+    *used = false;
+    if (graphs_off) return WOTG_OK;
+    if (!gs) {
+      if (cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&gev[0], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&gev[1], cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        release_graphs();
+        graphs_off = true;
+        return WOTG_OK;
+      }
+    }
+    BatchGraph& G = bg[parity & 1];
+    if (G.exec && G.nb != nb) {
+      cudaGraphExecDestroy(G.exec);
+      G = BatchGraph{};
+    }
+    bool fresh = false;
+    if (!G.exec) {
+      const unsigned long long before = launches_so_far();
+      WOTG_CUDA(cudaStreamBeginCapture(gs, cudaStreamCaptureModeThreadLocal));
+      const cudaStream_t user = st;
+      st = gs;
+      int s = WOTG_OK;
+      int p = parity;
+      for (int t = 0; t < nb && s == WOTG_OK; ++t) {
+        s = iteration(c, t == 0, p);
+        if (s == WOTG_OK) s = absorb(c, tau, p);
+        p ^= 1;
+      }
+      st = user;
+      cudaGraph_t graph = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(gs, &graph);
+      if (s != WOTG_OK || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        if (s != WOTG_OK) return s;
+        set_last_error("cudaStreamEndCapture", e);
+        return WOTG_CUDA_ERROR;
+      }
+      const cudaError_t ei = cudaGraphInstantiate(&G.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ei != cudaSuccess) {
+        G.exec = nullptr;
+        set_last_error("cudaGraphInstantiate", ei);
+        return WOTG_CUDA_ERROR;
+      }
+      G.launches = launches_so_far() - before;   // counted at capture, for the first replay
+      G.nb = nb;
+      fresh = true;
+    }
+    WOTG_CUDA(cudaEventRecord(gev[0], st));
+    WOTG_CUDA(cudaStreamWaitEvent(gs, gev[0], 0));
+    WOTG_CUDA(cudaGraphLaunch(G.exec, gs));
+    WOTG_CUDA(cudaEventRecord(gev[1], gs));
+    WOTG_CUDA(cudaStreamWaitEvent(st, gev[1], 0));
+    if (!fresh) count_launches(G.launches);
+    *used = true;
+    return WOTG_OK;
+  }
+
   // Solver outputs for one solve: learned row sums (device), optionally the
   // dense coupling and potentials.
   int outputs(const Coef& c, bool no_div_j, double* tmap, double* row_sums, double* ubar,
@@ -968,7 +1111,9 @@ struct Solver {
       WOTG_LAUNCHED();
     }
     if (tmap) {
-      // every column in one wave of x blocks (its FP64 weight formed once per thread), rows over y
+      coupling_rows_kernel<<<vec_blocks(g.I), 256, 0, st>>>(g, V, c, log_scale);
+      WOTG_LAUNCHED();
+      // every column in one wave of x blocks (its weight read once per thread), rows over y
       dim3 grid((unsigned)std::min<int64_t>((g.J + 255) / 256, 65535), (unsigned)std::min<int64_t>(g.I, 128));
       coupling_kernel<<<grid, 256, 0, st>>>(C, g, V, c, log_scale, tmap);
       WOTG_LAUNCHED();
@@ -976,6 +1121,18 @@ struct Solver {
     return WOTG_OK;
   }
 };
+
+// Frees a solver's captured graphs, stream and events when its entry point
+// returns (every replay has completed by then: each batch is followed by a
+// duality-gap check that synchronises the stream).
+struct SolverGraphs {
+  Solver& s;
+  ~SolverGraphs() { s.release_graphs(); }
+};
+
+// Set for the duration of a no-alloc call: its solver creates no stream, event
+// or graph of its own (plain launches on the caller's stream only).
+static thread_local bool t_plain_launches = false;
 
 struct SolveResult {
   int status = WOTG_OK;
@@ -1017,9 +1174,20 @@ static int solve_duality_gap(Solver& S, const wotg_params& P, double q, SolveRes
       s = S.sum_exp(c, &sumK);
       if (s) return s;
     }
+    S.drop_graphs();
     while (gap > threshold) {
       const int nb = final ? P.batch_size : 5;
-      for (int t = 0; t < nb; ++t) {
+      bool replayed = false;
+      if (final && lrow_valid && S.steady() && (double)(it + nb) < P.max_iter) {
+        s = S.batch_graph(c, nb, parity, P.tau, &replayed);
+        if (s) return s;
+      }
+      if (replayed) {
+        it += nb;
+        lrow_valid = false;
+        parity ^= (nb & 1);
+      }
+      for (int t = 0; t < nb && !replayed; ++t) {
         ++it;
         s = S.iteration(c, lrow_valid, parity);
         if (s) return s;
@@ -1158,6 +1326,7 @@ static size_t layout(Bump& b, const Geom& g, Vecs& V) {
   V.lb = b.take<double>(g.J);
   V.lb_old = b.take<double>(g.J);
   V.Lcol = b.take<double>(g.J);
+  V.rowc = b.take<float4>(g.I);
   V.wrow = b.take<float>(g.I);
   V.wcol = b.take<float>(g.ldc);
   V.wrow_lo = b.take<float>(g.I);
@@ -1306,6 +1475,8 @@ extern "C" int wotg_compute_transport_matrix(const wotg_problem* prob, const wot
   layout(b, g, V);
   cudaStream_t st = (cudaStream_t)stream;
   Solver S{prob->C, g, V, st, prob->cost_scale, 0, TcState{}};
+  SolverGraphs graphs_guard{S};
+  S.graphs_off = t_plain_launches;
   if (tc_requested(prob)) {
     tc_layout(b, prob, S.tc);
     WOTG_CUDA(cudaMemsetAsync(S.tc.err, 0, sizeof(int), st));
@@ -1400,6 +1571,8 @@ extern "C" int wotg_refine_potentials(const wotg_problem* prob, const wotg_param
   layout(b, g, V);
   cudaStream_t st = (cudaStream_t)stream;
   Solver S{prob->C, g, V, st, prob->cost_scale, 0, TcState{}};
+  SolverGraphs graphs_guard{S};
+  S.graphs_off = t_plain_launches;
   if (tc_requested(prob)) {
     tc_layout(b, prob, S.tc);
     WOTG_CUDA(cudaMemsetAsync(S.tc.err, 0, sizeof(int), st));
@@ -1518,6 +1691,10 @@ extern "C" int wotg_compute_transport_matrix_noalloc(const wotg_problem* prob, c
     WOTG_CUDA(cudaGetSymbolAddress(&scratch, g_noalloc_scratch));
     g_noalloc_ptr[dev].store(scratch, std::memory_order_release);
   }
+  struct Plain {
+    Plain() { t_plain_launches = true; }
+    ~Plain() { t_plain_launches = false; }
+  } plain;
   return wotg_compute_transport_matrix(prob, params, tmap, learned_growth, row_sums, u_bar, v_bar, stats,
                                        scratch, kNoAllocScratchBytes, stream);
 }
