@@ -420,6 +420,14 @@ int wotg_ot_adjoint(const float* X, int64_t I, int64_t ldx, const float* Y, int6
                     const double* v_bar, const double* p, double* grad_x, double* grad_y, double* grad_p,
                     double* objective, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Diagnostic (no counterpart in the reference): the replay profile of the last
+ * wotg_solve_batched call on this host thread, one record per graph replay
+ * (8 iterations of the whole batch): the number of items still active after
+ * the previous replay and the host milliseconds between the waits on
+ * successive replays (one replay's device time once the GPU is the bound).
+ * Writes min(cap, n) records (either array may be NULL), returns n. */
+int32_t wotg_batch_replay_profile(int32_t* active, float* ms, int32_t cap);
+
 /* Diagnostic (no counterpart in the reference): this GPU's measured throughput
  * of ex2.approx.ftz.f32 (exp2 per second, a register-only kernel timed with CUDA
  * events on `stream`, best of 3). Every half-step form spends one exp2 per cost

@@ -41,7 +41,7 @@ EXPORTS = (
     'wotg_batch_pass_timing', 'wotg_gemm_f64', 'wotg_csr_count', 'wotg_csr_fill',
     'wotg_csr_transpose_workspace_bytes', 'wotg_csr_transpose', 'wotg_spmm_centred', 'wotg_gram_workspace_bytes',
     'wotg_gram_f64', 'wotg_vecmat_workspace_bytes', 'wotg_vecmat_f64', 'wotg_apply_points_workspace_bytes',
-    'wotg_apply_points', 'wotg_exp2_fma',
+    'wotg_apply_points', 'wotg_exp2_fma', 'wotg_batch_replay_profile',
 )
 
 
@@ -146,6 +146,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         'wotg_ot_adjoint_workspace_bytes': (ctypes.c_size_t, [i64, i64]),
         'wotg_exp2_rate': (ctypes.c_int, [ctypes.POINTER(dbl), vp]),
         'wotg_exp2_fma': (ctypes.c_int, [vp, vp, i64, vp]),
+        'wotg_batch_replay_profile': (i32, [vp, vp, i32]),
         'wotg_lse_points_timing': (ctypes.c_int, [vp, i64, i64, vp, i64, i64, i32, dbl, vp, i32, i32,
                                                   ctypes.POINTER(ctypes.c_float), vp, ctypes.c_size_t, vp]),
         'wotg_refine_potentials': (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Params), dbl, i32, vp, vp,

@@ -33,6 +33,7 @@
 // (wotg_sinkhorn.cu) step for step, so every item gives the reference's
 // sequence of stages, checks and absorptions.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1192,6 +1193,10 @@ struct Tuned {
 };
 static std::map<TuneKey, Tuned> g_tuned;
 static std::mutex g_tune_mu;
+// Replay profile of the last wotg_solve_batched call on this host thread:
+// (active items read after replay n - 1, host milliseconds between successive
+// waits) per replay (diagnostic, wotg_batch_replay_profile).
+static thread_local std::vector<std::pair<int, float>> g_replay_prof;
 // The last batch's choice and measured pass time per direction (wotg_batch_pass_timing).
 static Tuned g_last_tuned[2] = {{-1, 0.f}, {-1, 0.f}};
 
@@ -1494,6 +1499,8 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
     max_iters = std::max(max_iters, items[k].params.max_iter * std::max(1, items[k].params.growth_iters));
   const double max_launches = std::min(max_iters, 1e12) / kBodies + 4;
   long long launched = 0;
+  g_replay_prof.clear();
+  auto t_last = std::chrono::steady_clock::now();
   for (;;) {
     const int slot = (int)(launched & 1);
     WOTG_BCUDA(cudaGraphLaunch(exec, cs));
@@ -1504,6 +1511,12 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
     if (launched >= 2) {
       const int prev = slot ^ 1;
       WOTG_BCUDA(cudaEventSynchronize(ev_done[prev]));
+      // replay profile: the host waits on replay n - 1 while replay n runs, so the
+      // interval between these waits is one replay's device time once GPU-bound
+      const auto t_now = std::chrono::steady_clock::now();
+      g_replay_prof.push_back(std::make_pair(pinned[prev],
+                                             std::chrono::duration<float, std::milli>(t_now - t_last).count()));
+      t_last = t_now;
       if (pinned[prev] == 0) break;
     }
     if ((double)launched > max_launches) {
@@ -1542,6 +1555,15 @@ extern "C" int wotg_solve_batched(const wotg_pair* pairs, int32_t n_pairs, const
   cleanup();
 #undef WOTG_BCUDA
   return status;
+}
+
+extern "C" int32_t wotg_batch_replay_profile(int32_t* active, float* ms, int32_t cap) {
+  const int32_t n = (int32_t)std::min<size_t>(g_replay_prof.size(), (size_t)std::max(0, cap));
+  for (int32_t k = 0; k < n; ++k) {
+    if (active) active[k] = g_replay_prof[k].first;
+    if (ms) ms[k] = g_replay_prof[k].second;
+  }
+  return (int32_t)g_replay_prof.size();
 }
 
 extern "C" size_t wotg_lse_matvec_multi_workspace_bytes(int64_t I, int32_t K) {

@@ -5,6 +5,8 @@
 #include <stdint.h>
 #include <math.h>
 
+#include <utility>
+
 #include "../../include/wotg.h"
 
 namespace wotg {
@@ -96,6 +98,15 @@ __device__ __forceinline__ double lse2(float o, float s) {
   }
   return (double)o + (double)e + (double)log2f(m);
 }
+
+// Programmatic dependent launch. A kernel launched with launch_dependent()
+// may be scheduled while the kernel before it in the stream still runs: it
+// calls pdl_wait() before touching any global memory (the wait returns once
+// that kernel has completed and its writes are visible; without the launch
+// attribute it returns at once), then pdl_trigger() to let the next dependent
+// launch be scheduled in turn.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // Streaming 128-bit load that is not kept in L1 (each cost element is read
 // once per pass; the matrix is far larger than L2).
@@ -208,5 +219,23 @@ struct Bump {
 };
 
 int sm_count();
+
+// Launch with programmatic stream serialisation (see pdl_wait): the launch's
+// latency and the kernel's prologue overlap the tail of the previous kernel.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                             Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 }  // namespace wotg

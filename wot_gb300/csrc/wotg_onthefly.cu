@@ -364,6 +364,10 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) lse_tc_kernel(const 
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
+  // launched as a dependent of the previous half-step's combine: everything
+  // above is this CTA's own set-up; global memory only from here on
+  pdl_wait();
+  pdl_trigger();
   const uint32_t tmem = *tmem_slot;
   const uint32_t sA = tc::smem_u32(smem + L::kA);
   const uint32_t sB = tc::smem_u32(smem + L::kB);
@@ -610,15 +614,25 @@ int tc_ctas_per_sm(int kp) {
 int tc_parts() { return kTcParts; }
 
 int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int kp, int ctas, float2* part,
-                  const float* off, int* err, cudaStream_t st, uint32_t wait_tries) {
+                  const float* off, int* err, cudaStream_t st, uint32_t wait_tries, bool dependent) {
+  const float* no_w = nullptr;
+  float* no_s = nullptr;
   if (kp == 32) {
     WOTG_CUDA(tc_set_smem_attr<32>());
-    lse_tc_kernel<32, 0><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
-                                                                        wait_tries, nullptr, 0, 0, nullptr);
+    if (dependent)
+      WOTG_CUDA(launch_dependent(lse_tc_kernel<32, 0>, dim3(ctas), dim3(kTcThreads), TcSmem<32>::kAlloc, st, Pt, Qt,
+                                 n_ptiles, nq, part, off, err, wait_tries, no_w, 0, 0, no_s));
+    else
+      lse_tc_kernel<32, 0><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
+                                                                          wait_tries, nullptr, 0, 0, nullptr);
   } else if (kp == 64) {
     WOTG_CUDA(tc_set_smem_attr<64>());
-    lse_tc_kernel<64, 0><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
-                                                                        wait_tries, nullptr, 0, 0, nullptr);
+    if (dependent)
+      WOTG_CUDA(launch_dependent(lse_tc_kernel<64, 0>, dim3(ctas), dim3(kTcThreads), TcSmem<64>::kAlloc, st, Pt, Qt,
+                                 n_ptiles, nq, part, off, err, wait_tries, no_w, 0, 0, no_s));
+    else
+      lse_tc_kernel<64, 0><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
+                                                                          wait_tries, nullptr, 0, 0, nullptr);
   } else {
     return WOTG_BADARG;
   }

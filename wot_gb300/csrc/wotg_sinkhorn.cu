@@ -391,6 +391,8 @@ __global__ void col_combine_kernel(Geom g, Vecs V, Coef c, int parity) {
 // The on-the-fly form also rewrites the column-form biases of the absorbed
 // points (bx, by; tiles = nullptr in the materialised form).
 __global__ void absorb_kernel(Geom g, Vecs V, Coef c, double tau, int parity, TcBias bx, TcBias by) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const double mx = __longlong_as_double((long long)V.maxslot[parity]);
   if (idx == 0) V.maxslot[parity ^ 1] = 0ull;
@@ -737,6 +739,8 @@ __global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restri
                                   int nparts, const double* __restrict__ norm, int parity, int spec,
                                   float* __restrict__ off, int* __restrict__ redo, int* __restrict__ redo_other,
                                   TcBias bias) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t n = ROW ? g.I : g.J;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   // the other side's list of exactly recomputed rows was consumed by its last
@@ -788,6 +792,8 @@ __global__ void tc_exact_rows_kernel(Geom g, Vecs V, Coef c, const float* __rest
                                      const float* __restrict__ Q, int64_t ldq, int d, const double* __restrict__ norm,
                                      float* __restrict__ off, int* __restrict__ redo,
                                      unsigned long long* __restrict__ total, int parity, TcBias bias) {
+  pdl_wait();
+  pdl_trigger();
   const int cnt = redo[0];
   if (blockIdx.x == 0 && threadIdx.x == 0 && cnt > 0) atomicAdd(total, (unsigned long long)cnt);
   const int lane = threadIdx.x & 31;
@@ -884,17 +890,18 @@ struct Solver {
     }
     const bool spec = tc.off_row_ok;
     int s = tc_lse_launch(tc.Xa, tc.n_xt, tc.Yb, tc.n_yt, tc.kp, tc.ctas_row, tc.part, spec ? tc.offX : nullptr,
-                          tc.err, st);
+                          tc.err, st, kTcDefaultWaitTries, true);
     if (s) return s;
     const TcBias bx = UPDATE ? bias_x() : TcBias{};
-    tc_combine_kernel<true, UPDATE><<<(unsigned)((g.I + 63) / 64), 64, 0, st>>>(
-        g, V, c, tc.part, tc.n_yt, tc.ctas_row, tc_parts(), tc.normX, parity, spec ? 1 : 0, tc.offX, tc.redoX,
-        tc.redoY, bx);
+    const int sp = spec ? 1 : 0;
+    WOTG_CUDA(launch_dependent(tc_combine_kernel<true, UPDATE>, dim3((unsigned)((g.I + 63) / 64)), dim3(64), 0, st, g,
+                               V, c, (const float2*)tc.part, tc.n_yt, tc.ctas_row, tc_parts(),
+                               (const double*)tc.normX, parity, sp, tc.offX, tc.redoX, tc.redoY, bx));
     WOTG_LAUNCHED();
     if (spec) {
-      tc_exact_rows_kernel<true, UPDATE><<<2 * sm_count(), 256, 0, st>>>(g, V, c, tc.X, tc.ldx, tc.Y, tc.ldy, tc.d,
-                                                                       tc.normX, tc.offX, tc.redoX, tc.redo_total,
-                                                                       parity, bx);
+      WOTG_CUDA(launch_dependent(tc_exact_rows_kernel<true, UPDATE>, dim3(2 * sm_count()), dim3(256), 0, st, g, V, c,
+                                 (const float*)tc.X, tc.ldx, (const float*)tc.Y, tc.ldy, tc.d,
+                                 (const double*)tc.normX, tc.offX, tc.redoX, tc.redo_total, parity, bx));
       WOTG_LAUNCHED();
     }
     tc.off_row_ok = true;
@@ -909,16 +916,17 @@ struct Solver {
     }
     const bool spec = tc.off_col_ok;
     int s = tc_lse_launch(tc.Ya, tc.n_yt, tc.Xb, tc.n_xt, tc.kp, tc.ctas_col, tc.part, spec ? tc.offY : nullptr,
-                          tc.err, st);
+                          tc.err, st, kTcDefaultWaitTries, true);
     if (s) return s;
-    tc_combine_kernel<false, true><<<(unsigned)((g.J + 63) / 64), 64, 0, st>>>(
-        g, V, c, tc.part, tc.n_xt, tc.ctas_col, tc_parts(), tc.normY, parity, spec ? 1 : 0, tc.offY, tc.redoY,
-        tc.redoX, bias_y());
+    const int sp = spec ? 1 : 0;
+    WOTG_CUDA(launch_dependent(tc_combine_kernel<false, true>, dim3((unsigned)((g.J + 63) / 64)), dim3(64), 0, st, g,
+                               V, c, (const float2*)tc.part, tc.n_xt, tc.ctas_col, tc_parts(),
+                               (const double*)tc.normY, parity, sp, tc.offY, tc.redoY, tc.redoX, bias_y()));
     WOTG_LAUNCHED();
     if (spec) {
-      tc_exact_rows_kernel<false, true><<<2 * sm_count(), 256, 0, st>>>(g, V, c, tc.Y, tc.ldy, tc.X, tc.ldx, tc.d,
-                                                                      tc.normY, tc.offY, tc.redoY, tc.redo_total,
-                                                                      parity, bias_y());
+      WOTG_CUDA(launch_dependent(tc_exact_rows_kernel<false, true>, dim3(2 * sm_count()), dim3(256), 0, st, g, V, c,
+                                 (const float*)tc.Y, tc.ldy, (const float*)tc.X, tc.ldx, tc.d,
+                                 (const double*)tc.normY, tc.offY, tc.redoY, tc.redo_total, parity, bias_y()));
       WOTG_LAUNCHED();
     }
     tc.off_col_ok = true;
@@ -954,8 +962,11 @@ struct Solver {
   }
 
   int absorb(const Coef& c, double tau, int parity) {
-    absorb_kernel<<<vec_blocks(g.I + g.J), 256, 0, st>>>(g, V, c, tau, parity, tc.on ? bias_x() : TcBias{},
-                                                         tc.on ? bias_y() : TcBias{});
+    if (tc.on)
+      WOTG_CUDA(launch_dependent(absorb_kernel, dim3(vec_blocks(g.I + g.J)), dim3(256), 0, st, g, V, c, tau, parity,
+                                 bias_x(), bias_y()));
+    else
+      absorb_kernel<<<vec_blocks(g.I + g.J), 256, 0, st>>>(g, V, c, tau, parity, TcBias{}, TcBias{});
     WOTG_LAUNCHED();
     return WOTG_OK;
   }
@@ -1070,18 +1081,16 @@ struct Solver {
       st = user;
       cudaGraph_t graph = nullptr;
       const cudaError_t e = cudaStreamEndCapture(gs, &graph);
-      if (s != WOTG_OK || e != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        if (s != WOTG_OK) return s;
-        set_last_error("cudaStreamEndCapture", e);
-        return WOTG_CUDA_ERROR;
-      }
-      const cudaError_t ei = cudaGraphInstantiate(&G.exec, graph, 0);
-      cudaGraphDestroy(graph);
-      if (ei != cudaSuccess) {
-        G.exec = nullptr;
-        set_last_error("cudaGraphInstantiate", ei);
-        return WOTG_CUDA_ERROR;
+      cudaError_t ei = e;
+      if (s == WOTG_OK && e == cudaSuccess) ei = cudaGraphInstantiate(&G.exec, graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+      if (s != WOTG_OK || ei != cudaSuccess) {
+        // nothing of the batch ran (capture only) and the host state is the one
+        // it started from: fall back to plain launches for the rest of the solve
+        G = BatchGraph{};
+        cudaGetLastError();
+        graphs_off = true;
+        return WOTG_OK;
       }
       G.launches = launches_so_far() - before;   // counted at capture, for the first replay
       G.nb = nb;
