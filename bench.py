@@ -985,7 +985,8 @@ def main():
         line['e2e'] = {'value': world * args.steps / te, 'unit': 'maps/s',
                        'h2d_bytes_per_step': int(X.shape[0] * X.shape[1] * 8 + I_FULL * 8),
                        'd2h_bytes_per_step': int(I_FULL * J_FULL * 8 + 3 * I_FULL * 8),
-                       'api': 'wot_gb300.OTModel(Dataset).compute_transport_map(0, 1) (device PCA + cost + solve)'}
+                       'api': 'wot_gb300.OTModel(Dataset).compute_transport_map(0, 1) (device PCA + cost + solve)',
+                       'last_call_s': getattr(model, 'last_timing', None)}
     if rank == 0 and not args.no_cpu:
         rng = np.random.default_rng(0)
         a_h, b_h, G_h = a.double().cpu().numpy(), b.double().cpu().numpy(), growth[day == 0]

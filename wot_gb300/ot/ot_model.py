@@ -13,6 +13,7 @@ from __future__ import annotations
 import itertools
 import logging
 import os
+import time
 from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
@@ -323,6 +324,7 @@ class OTModel:
             logger.info('No cells at {}'.format(t1))
             return None
         local_pca = config.pop('local_pca', None)
+        clock = [('start', time.perf_counter())]
         if config['C'] is None:
             if local_pca is not None and local_pca > 0:
                 x0, x1, s, _ = compute_pca(p0.X, p1.X, local_pca, solver=self.pca)
@@ -338,12 +340,18 @@ class OTModel:
             config['G'] = np.ones(n0)
         sid = ot.native_solver_id(self.solver)
         cost = C if isinstance(C, D.DeviceCost) else D.cost_from_dense(C)
+        clock.append(('pca_cost', time.perf_counter()))
         # the host array of the FP64 map is allocated and its pages faulted in on
         # host threads while the GPU works; the copy into it then runs at link speed
         out = _prefaulted_async(C.shape[0], C.shape[1])
         res = D.solve(cost, config['G'], config, sid, want_tmap=True, form=self.form)
+        clock.append(('solve', time.perf_counter()))
         tmap = out.result()
+        clock.append(('host_pages_wait', time.perf_counter()))
         N.require_cuda().from_numpy(tmap).copy_(res.tmap)
+        clock.append(('copy_to_host', time.perf_counter()))
+        # seconds per stage of this call (the solve returns after its device work)
+        self.last_timing = {k: clock[i + 1][1] - clock[i][1] for i, (k, _) in enumerate(clock[1:])}
         learned = [np.asarray(config['G'], dtype=np.float64)] + [g.cpu().numpy() for g in res.learned_growth[1:]]
         learned.append(res.row_sums.cpu().numpy())
         obs_growth = {'g' + str(i): np.power(g, 1.0 / delta_days) for i, g in enumerate(learned)}
