@@ -35,6 +35,7 @@
 #include "wotg_coef.cuh"
 #include "wotg_common.cuh"
 #include "wotg_onthefly.cuh"
+#include "wotg_tc_kernel.cuh"
 
 namespace wotg {
 
@@ -89,15 +90,16 @@ struct TcState {
   // from the previous half-step (row side offX, column side offY), valid while
   // epsilon is unchanged; rows whose sum left the safe range are listed in
   // redoX / redoY = [count, rows...] (row and column passes) and recomputed
-  // exactly; each side's combine empties the other side's list.
+  // exactly; each side's half-step empties the other side's list.
   float* offX;
   float* offY;
   int* redoX;
   int* redoY;
+  int* tile_ctr;                   // per (row tile, lane quarter): partials written (CombineFin)
   unsigned long long* redo_total;  // rows recomputed exactly, over the solve (diagnostic)
   bool off_row_ok, off_col_ok;
   // Column-form biases of X (read by column passes) and Y (row passes) match
-  // the current potentials: written by the combine of the half-step that
+  // the current potentials: written by the row-tile finish of the half-step that
   // updated them, else packed before the pass that reads them.
   bool xb_ok, yb_ok;
 };
@@ -712,18 +714,14 @@ __global__ void __launch_bounds__(256) coupling_kernel(const float* __restrict__
 }
 
 // ---------------------------------------------------------------------------
-// On-the-fly form: the FP64 merge of the tensor-core kernel's partials. The
+// On-the-fly form: the FP64 finish of the tensor-core kernel's partials. The
 // exponent of element (i, j) is split as
 //   bias_j + gamma (x_i . y_j) - kappa2 |x_i|^2,   gamma = 2 kappa2,
 //   bias_j = (v_j / eps + lb_j) log2 e - kappa2 |y_j|^2     (FP64, carried by the MMA),
 // i.e. (v_j/eps + lb_j - kappa C_ij) in base 2 with C = |x|^2 + |y|^2 - 2 x.y; the
-// tensor-core kernel produces the first two terms, the merge adds the third.
+// tensor-core kernel produces the first two terms, its row-tile finish
+// (CombineFin, below) adds the third.
 // ---------------------------------------------------------------------------
-// Merge of the tensor-core kernel's partials: one thread per point, over the
-// (CTA, column quarter) partials whose stretch covered the point's row tile
-// (FP32 LSE merge), then the FP64 finish and update. Launched in 64-thread
-// blocks: the per-row FP64 work is latency-bound, so spreading the rows over
-// every SM beats fewer, fuller blocks.
 // Column-form bias of point i of the side a half-step just updated (ROW: a row
 // point with its new log-scaling la, for the next column pass; else a column
 // point with its new lb, for the next row pass).
@@ -734,59 +732,9 @@ __device__ __forceinline__ void write_bias(int64_t i, const Vecs& V, const Coef&
   tc_write_bias(i, (pot * c.inv_eps + lsc) * kLog2e - (c.kappa * kLog2e) * b.norm[i], b.d, b.kp, b.tiles);
 }
 
-template <bool ROW, bool UPDATE>
-__global__ void tc_combine_kernel(Geom g, Vecs V, Coef c, const float2* __restrict__ part, int nq, int ctas,
-                                  int nparts, const double* __restrict__ norm, int parity, int spec,
-                                  float* __restrict__ off, int* __restrict__ redo, int* __restrict__ redo_other,
-                                  TcBias bias) {
-  pdl_wait();
-  pdl_trigger();
-  const int64_t n = ROW ? g.I : g.J;
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  // the other side's list of exactly recomputed rows was consumed by its last
-  // half-step (earlier in the stream): empty it for that side's next one
-  if (i == 0) redo_other[0] = 0;
-  double vmax = 0.0;
-  bool skip = false;
-  if (i < n) {
-    const int64_t t = i >> 7;
-    const int64_t total = (((n + 127) >> 7)) * (int64_t)nq;
-    const int64_t c_lo = tc_cta_of(t * nq, total, ctas);
-    const int64_t c_hi = tc_cta_of((t + 1) * nq - 1, total, ctas);
-    float m = kNegBig, s = 0.f;
-    for (int64_t cc = c_lo; cc <= c_hi; ++cc) {
-      const float2* pp = part + ((cc + t) * 128 + (i & 127)) * nparts;
-      for (int k = 0; k < nparts; ++k) {
-        const float2 u = pp[k];
-        lse_merge(m, s, u.x, u.y);
-      }
-    }
-    if (spec && !(s >= 0x1p-80f && s <= 0x1p100f)) {
-      // outside the speculative form's safe range: recomputed exactly
-      const int k = atomicAdd(redo, 1);
-      redo[1 + k] = (int)i;
-      skip = true;
-    } else {
-      const double D = lse2(m, s);
-      off[i] = (float)D;
-      const double L = D * kLn2 - c.kappa * norm[i];
-      if (ROW) {
-        V.Lrow[i] = L;
-        if (UPDATE) vmax = a_update(i, L, V, c);
-      } else {
-        V.Lcol[i] = L;
-        if (UPDATE) vmax = b_update(i, L, V, c);
-      }
-      if (UPDATE && bias.tiles) write_bias<ROW>(i, V, c, bias);
-    }
-  }
-  (void)skip;
-  if (UPDATE) block_max_to_slot(vmax, V.maxslot + parity);
-}
-
-// Exact half-step of the rows listed by a speculative combine (a warp per row):
+// Exact half-step of the rows listed by a speculative half-step (a warp per row):
 // L_i = log sum_j exp(w_j - kappa |x_i - y_j|^2) from the FP32 points with a
-// running maximum, then the same update and offset as the combine.
+// running maximum, then the same update and offset as the row-tile finish.
 template <bool ROW, bool UPDATE>
 __global__ void tc_exact_rows_kernel(Geom g, Vecs V, Coef c, const float* __restrict__ P, int64_t ldp,
                                      const float* __restrict__ Q, int64_t ldq, int d, const double* __restrict__ norm,
@@ -836,6 +784,83 @@ __global__ void tc_exact_rows_kernel(Geom g, Vecs V, Coef c, const float* __rest
   }
 }
 
+// Row-tile finish of an on-the-fly half-step inside lse_tc_kernel: the warp
+// that writes the last partial of 32 rows (over the CTAs and column halves that
+// covered their row tile) merges them in a fixed order (FP32 LSE merge), then
+// per row either lists it for the exact recompute (a speculative sum outside
+// [2^-80, 2^100]) or writes its offset and log-sum-exp and, with UPDATE, the
+// FP64 a- or b-update, the point's column-form bias for the other side's next
+// pass and the absorption maximum (the work of a separate merge pass, without
+// its launch and its wait on the whole kernel). Ordering: every lane fences its partial, the warp synchronises, one
+// atomic per warp counts it; the finishing warp fences again and reads the
+// partials from L2.
+template <bool ROW, bool UPDATE>
+struct CombineFin {
+  static constexpr bool kActive = true;
+  Geom g;
+  Vecs V;
+  Coef c;
+  const double* norm;
+  float* off;
+  int* redo;
+  int* redo_other;
+  TcBias bias;
+  int* ctr;  // per (row tile, lane quarter): partials written so far
+  int nq, ctas, parity, spec;
+
+  // the other side's exact-row list was consumed by its last half-step
+  __device__ __forceinline__ void start() const { redo_other[0] = 0; }
+
+  __device__ void quarter_done(const float2* part, int t, int wq, int lane) const {
+    __threadfence();
+    __syncwarp();
+    const int64_t n = ROW ? g.I : g.J;
+    const int64_t total = ((n + 127) >> 7) * (int64_t)nq;
+    const int64_t c_lo = tc_cta_of((int64_t)t * nq, total, ctas);
+    const int64_t c_hi = tc_cta_of(((int64_t)t + 1) * nq - 1, total, ctas);
+    const int expect = 2 * (int)(c_hi - c_lo + 1);
+    int old = 0;
+    if (lane == 0) old = atomicAdd(ctr + 4 * t + wq, 1);
+    old = __shfl_sync(0xffffffffu, old, 0);
+    if (old != expect - 1) return;
+    if (lane == 0) ctr[4 * t + wq] = 0;   // for the next launch
+    __threadfence();
+    const int64_t i = (int64_t)t * 128 + 32 * wq + lane;
+    double vmax = 0.0;
+    if (i < n) {
+      float m = kNegBig, s = 0.f;
+      for (int64_t cc = c_lo; cc <= c_hi; ++cc) {
+        const float2* pp = part + ((cc + t) * 128 + (i & 127)) * kTcParts;
+#pragma unroll
+        for (int k = 0; k < kTcParts; ++k) {
+          const float2 u = __ldcg(pp + k);
+          lse_merge(m, s, u.x, u.y);
+        }
+      }
+      if (spec && !(s >= 0x1p-80f && s <= 0x1p100f)) {
+        const int k = atomicAdd(redo, 1);
+        redo[1 + k] = (int)i;
+      } else {
+        const double D = lse2(m, s);
+        off[i] = (float)D;
+        const double L = D * kLn2 - c.kappa * norm[i];
+        if (ROW) {
+          V.Lrow[i] = L;
+          if (UPDATE) vmax = a_update(i, L, V, c);
+        } else {
+          V.Lcol[i] = L;
+          if (UPDATE) vmax = b_update(i, L, V, c);
+        }
+        if (UPDATE && bias.tiles) write_bias<ROW>(i, V, c, bias);
+      }
+    }
+    if (UPDATE) {
+      vmax = warp_maxd(vmax);
+      if (lane == 0) atomic_max_nonneg(V.maxslot + parity, vmax);
+    }
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
@@ -869,6 +894,7 @@ struct Solver {
     tc.xb_ok = tc.yb_ok = false;
     WOTG_CUDA(cudaMemsetAsync(tc.redoX, 0, sizeof(int), st));
     WOTG_CUDA(cudaMemsetAsync(tc.redoY, 0, sizeof(int), st));
+    WOTG_CUDA(cudaMemsetAsync(tc.tile_ctr, 0, sizeof(int) * 4 * std::max(tc.n_xt, tc.n_yt), st));
     const float gamma = (float)(2.0 * c.kappa * kLog2e / std::sqrt(cost_scale));
     int s = tc_pack_points(tc.X, g.I, tc.ldx, tc.d, tc.kp, gamma, 1, tc.Xa, nullptr, st);
     if (s) return s;
@@ -881,6 +907,44 @@ struct Solver {
   TcBias bias_x() const { return TcBias{tc.Xb, tc.normX, tc.d, tc.kp}; }
   TcBias bias_y() const { return TcBias{tc.Yb, tc.normY, tc.d, tc.kp}; }
 
+  // One on-the-fly half-step with its row-tile finish inside the kernel
+  // (CombineFin), launched as a dependent of the previous kernel.
+  template <bool ROW, bool UPDATE>
+  int tc_fused_pass(const Coef& c, int parity, bool spec) {
+    using F = CombineFin<ROW, UPDATE>;
+    F fin;
+    fin.g = g;
+    fin.V = V;
+    fin.c = c;
+    fin.norm = ROW ? tc.normX : tc.normY;
+    fin.off = ROW ? tc.offX : tc.offY;
+    fin.redo = ROW ? tc.redoX : tc.redoY;
+    fin.redo_other = ROW ? tc.redoY : tc.redoX;
+    fin.bias = UPDATE ? (ROW ? bias_x() : bias_y()) : TcBias{};
+    fin.ctr = tc.tile_ctr;
+    fin.nq = ROW ? tc.n_yt : tc.n_xt;
+    fin.ctas = ROW ? tc.ctas_row : tc.ctas_col;
+    fin.parity = parity;
+    fin.spec = spec ? 1 : 0;
+    const __half* Pt = ROW ? tc.Xa : tc.Ya;
+    const __half* Qt = ROW ? tc.Yb : tc.Xb;
+    const int n_pt = ROW ? tc.n_xt : tc.n_yt;
+    const float* offp = spec ? fin.off : nullptr;
+    const float* no_w = nullptr;
+    float* no_s = nullptr;
+    if (tc.kp == 32) {
+      WOTG_CUDA((tc_set_smem_attr<32, 0, F>()));
+      WOTG_CUDA(launch_dependent(lse_tc_kernel<32, 0, F>, dim3(fin.ctas), dim3(kTcThreads), TcSmem<32>::kAlloc, st,
+                                 Pt, Qt, n_pt, fin.nq, tc.part, offp, tc.err, kTcWaitTries, no_w, 0, 0, no_s, fin));
+    } else {
+      WOTG_CUDA((tc_set_smem_attr<64, 0, F>()));
+      WOTG_CUDA(launch_dependent(lse_tc_kernel<64, 0, F>, dim3(fin.ctas), dim3(kTcThreads), TcSmem<64>::kAlloc, st,
+                                 Pt, Qt, n_pt, fin.nq, tc.part, offp, tc.err, kTcWaitTries, no_w, 0, 0, no_s, fin));
+    }
+    WOTG_LAUNCHED();
+    return WOTG_OK;
+  }
+
   template <bool UPDATE>
   int tc_row_pass(const Coef& c, int parity) {
     if (!tc.yb_ok) {
@@ -889,15 +953,9 @@ struct Solver {
       tc.yb_ok = true;
     }
     const bool spec = tc.off_row_ok;
-    int s = tc_lse_launch(tc.Xa, tc.n_xt, tc.Yb, tc.n_yt, tc.kp, tc.ctas_row, tc.part, spec ? tc.offX : nullptr,
-                          tc.err, st, kTcDefaultWaitTries, true);
+    int s = tc_fused_pass<true, UPDATE>(c, parity, spec);
     if (s) return s;
     const TcBias bx = UPDATE ? bias_x() : TcBias{};
-    const int sp = spec ? 1 : 0;
-    WOTG_CUDA(launch_dependent(tc_combine_kernel<true, UPDATE>, dim3((unsigned)((g.I + 63) / 64)), dim3(64), 0, st, g,
-                               V, c, (const float2*)tc.part, tc.n_yt, tc.ctas_row, tc_parts(),
-                               (const double*)tc.normX, parity, sp, tc.offX, tc.redoX, tc.redoY, bx));
-    WOTG_LAUNCHED();
     if (spec) {
       WOTG_CUDA(launch_dependent(tc_exact_rows_kernel<true, UPDATE>, dim3(2 * sm_count()), dim3(256), 0, st, g, V, c,
                                  (const float*)tc.X, tc.ldx, (const float*)tc.Y, tc.ldy, tc.d,
@@ -915,14 +973,8 @@ struct Solver {
       tc.xb_ok = true;
     }
     const bool spec = tc.off_col_ok;
-    int s = tc_lse_launch(tc.Ya, tc.n_yt, tc.Xb, tc.n_xt, tc.kp, tc.ctas_col, tc.part, spec ? tc.offY : nullptr,
-                          tc.err, st, kTcDefaultWaitTries, true);
+    int s = tc_fused_pass<false, true>(c, parity, spec);
     if (s) return s;
-    const int sp = spec ? 1 : 0;
-    WOTG_CUDA(launch_dependent(tc_combine_kernel<false, true>, dim3((unsigned)((g.J + 63) / 64)), dim3(64), 0, st, g,
-                               V, c, (const float2*)tc.part, tc.n_xt, tc.ctas_col, tc_parts(),
-                               (const double*)tc.normY, parity, sp, tc.offY, tc.redoY, tc.redoX, bias_y()));
-    WOTG_LAUNCHED();
     if (spec) {
       WOTG_CUDA(launch_dependent(tc_exact_rows_kernel<false, true>, dim3(2 * sm_count()), dim3(256), 0, st, g, V, c,
                                  (const float*)tc.Y, tc.ldy, (const float*)tc.X, tc.ldx, tc.d,
@@ -1426,6 +1478,7 @@ static void tc_layout(Bump& b, const wotg_problem* prob, TcState& tc) {
   tc.offY = b.take<float>(tc.J_pad);
   tc.redoX = b.take<int>(2 + prob->I);
   tc.redoY = b.take<int>(2 + prob->J);
+  tc.tile_ctr = b.take<int>((size_t)4 * std::max(tc.n_xt, tc.n_yt));
   tc.redo_total = b.take<unsigned long long>(1);
   tc.off_row_ok = tc.off_col_ok = false;
   tc.xb_ok = tc.yb_ok = false;
