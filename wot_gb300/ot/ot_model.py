@@ -313,6 +313,7 @@ class OTModel:
         if t0 is None or t1 is None:
             raise ValueError("config must have both t0 and t1, indicating target timepoints")
         config['t0'], config['t1'] = t0, t1
+        clock = [('start', time.perf_counter())]
         p0, p1 = self.select_pair(config)
         config.pop('t0')
         config.pop('t1')
@@ -324,7 +325,7 @@ class OTModel:
             logger.info('No cells at {}'.format(t1))
             return None
         local_pca = config.pop('local_pca', None)
-        clock = [('start', time.perf_counter())]
+        clock.append(('select', time.perf_counter()))
         if config['C'] is None:
             if local_pca is not None and local_pca > 0:
                 x0, x1, s, _ = compute_pca(p0.X, p1.X, local_pca, solver=self.pca)
@@ -350,13 +351,16 @@ class OTModel:
         clock.append(('host_pages_wait', time.perf_counter()))
         N.require_cuda().from_numpy(tmap).copy_(res.tmap)
         clock.append(('copy_to_host', time.perf_counter()))
-        # seconds per stage of this call (the solve returns after its device work)
-        self.last_timing = {k: clock[i + 1][1] - clock[i][1] for i, (k, _) in enumerate(clock[1:])}
         learned = [np.asarray(config['G'], dtype=np.float64)] + [g.cpu().numpy() for g in res.learned_growth[1:]]
         learned.append(res.row_sums.cpu().numpy())
         obs_growth = {'g' + str(i): np.power(g, 1.0 / delta_days) for i, g in enumerate(learned)}
         self.last_stats = res.stats
-        return ds_.make_result(tmap, obs_growth, ds_.index(p0.obs), ds_.index(p1.obs), like=self.matrix)
+        result = ds_.make_result(tmap, obs_growth, ds_.index(p0.obs), ds_.index(p1.obs), like=self.matrix)
+        clock.append(('assemble', time.perf_counter()))
+        # seconds per stage of this call (the solve returns after its device work)
+        self.last_timing = {k: clock[i + 1][1] - clock[i][1] for i, (k, _) in enumerate(clock[1:])}
+        self.last_timing['call'] = clock[-1][1] - clock[0][1]
+        return result
 
 
 def _as_slice(mask):
