@@ -1010,7 +1010,11 @@ def main():
                                 'sample': '%dx%d random subsample of the pair, full FP64 oracle solve with 3 growth '
                                           'iterations (%.1f s, %d iterations); extrapolated to 20000x25000 by '
                                           'I*J*iterations' % (SAMPLE[0], SAMPLE[1], t_cpu, it_cpu),
-                                'sample_stages_s': {k: round(v, 3) for k, v in stages.items()}}
+                                'sample_stages_s': {k: round(v, 3) for k, v in stages.items()},
+                                'measured_whole_pair': dict(CPU_FULL_SIZE, note='the oracle on the whole '
+                                                            '20000x25000 pair, timed once on this host type '
+                                                            '(growth_iters=1); per iteration 1.38x the '
+                                                            'extrapolation, so value is an upper bound')}
     if rank == 0 and not args.no_parity:
         # the whole pair against the reference's solver in FP64 (same coordinates, all growth iterations)
         G_dev = growth[day == 0]
