@@ -366,31 +366,3 @@ def test_objective_helpers_match_the_reference_forms():
     if not torch.cuda.is_available():
         with pytest.raises(RuntimeError, match='CUDA device'):
             wot_gb300.ot.primal(C, K, R, dx, dy, p, q, a, b, eps, l1, l2)
-
-
-def test_host_map_buffers_are_reused_only_when_released():
-    """The FP64 map arrays handed to callers: a buffer is reused for the next map
-    of the same size only once no array or view of it is alive; idle buffers
-    of other sizes are released."""
-    from wot_gb300.ot import ot_model as M
-    M.release_host_maps()
-    n0 = len(M._HOST_MAPS)
-    a = M._prefaulted_async(60, 40).result()
-    b = M._prefaulted_async(60, 40).result()
-    assert a.shape == (60, 40) and a.dtype == np.float64
-    assert a.base is not b.base
-    a[:] = 1.0
-    v = a[3:5]
-    del a
-    c = M._prefaulted_async(60, 40).result()
-    assert all(c.base is not x.base for x in (b, v))     # a view of the first is alive
-    del v
-    d = M._prefaulted_async(60, 40).result()
-    assert len(M._HOST_MAPS) == n0 + 3                    # the first buffer, reused
-    assert d.base is M._HOST_MAPS[n0]
-    del b, c, d
-    e = M._prefaulted_async(7, 9).result()
-    assert len(M._HOST_MAPS) == 1 and e.base is M._HOST_MAPS[0]
-    del e
-    M.release_host_maps()
-    assert len(M._HOST_MAPS) == 0

@@ -13,8 +13,6 @@ from __future__ import annotations
 import itertools
 import logging
 import os
-import sys
-import threading
 import time
 from concurrent.futures import ThreadPoolExecutor
 
@@ -375,71 +373,33 @@ def _as_slice(mask):
 
 
 _TOUCH_POOL = None
-# Backing buffers (uint8 arrays) of the FP64 maps handed to callers. A map array
-# is a view of its buffer; once the caller has dropped the map and every view
-# of it, only this list refers to the buffer, and the next map of the same size
-# reuses it: its pages are already faulted in, and no 4 GB region is unmapped
-# and mapped again per map. At most _KEEP_IDLE buffers wait here unused.
-_HOST_MAPS = []
-_HOST_MAPS_LOCK = threading.Lock()
-_KEEP_IDLE = 1
-
-
-def _idle(k):
-    # referenced only by _HOST_MAPS (and getrefcount's own argument)
-    return sys.getrefcount(_HOST_MAPS[k]) == 2
-
-
-class _MapFuture:
-    """The host map array of a call, ready once its pages are faulted in (no
-    closure or class cycle keeps the array alive after the caller drops it)."""
-    __slots__ = ('arr', 'futs')
-
-    def __init__(self, arr, futs=()):
-        self.arr = arr
-        self.futs = futs
-
-    def result(self):
-        for f in self.futs:
-            f.result()
-        return self.arr
-
-
-def _touch(flat, a, b):
-    flat[a:b:512] = 0.0   # one store per 4 KB of float64
 
 
 def _prefaulted_async(rows, cols, parts=8):
-    """Future of an uninitialised (rows x cols) FP64 array whose pages are
-    faulted in before the device-to-host copy: a released buffer of the same
-    size when there is one, else a new one whose pages are written once (one
-    store per 4 KB, spread over host threads) while the GPU works."""
+    """Future of an uninitialised (rows x cols) FP64 array whose pages have been
+    written once (one store per 4 KB, spread over host threads), so that a
+    device-to-host copy into it does not stop on first-touch page faults."""
+    from concurrent.futures import ThreadPoolExecutor
     global _TOUCH_POOL
-    nbytes = int(rows) * int(cols) * 8
-    with _HOST_MAPS_LOCK:
-        for k in range(len(_HOST_MAPS)):
-            if _HOST_MAPS[k].nbytes == nbytes and _idle(k):
-                return _MapFuture(_HOST_MAPS[k].view(np.float64).reshape(int(rows), int(cols)))
-        idle = [k for k in range(len(_HOST_MAPS)) if _idle(k)]
-        for k in reversed(idle[:max(0, len(idle) - (_KEEP_IDLE - 1))]):
-            del _HOST_MAPS[k]
-        base = np.empty(nbytes, dtype=np.uint8)
-        _HOST_MAPS.append(base)
     if _TOUCH_POOL is None:
         _TOUCH_POOL = ThreadPoolExecutor(max_workers=parts, thread_name_prefix='wotg-prefault')
-    arr = base.view(np.float64).reshape(int(rows), int(cols))
+    arr = np.empty((int(rows), int(cols)), dtype=np.float64)
     flat = arr.reshape(-1)
+    step = 512  # 4 KB of float64
     bounds = np.linspace(0, flat.size, parts + 1).astype(np.int64)
-    futs = [_TOUCH_POOL.submit(_touch, flat, int(bounds[k]), int(bounds[k + 1])) for k in range(parts)]
-    return _MapFuture(arr, futs)
 
+    def touch(a, b):
+        flat[a:b:step] = 0.0
 
-def release_host_maps():
-    """Free the cached map buffers that no caller holds any more."""
-    with _HOST_MAPS_LOCK:
-        for k in reversed(range(len(_HOST_MAPS))):
-            if _idle(k):
-                del _HOST_MAPS[k]
+    futs = [_TOUCH_POOL.submit(touch, int(bounds[k]), int(bounds[k + 1])) for k in range(parts)]
+
+    class _Result:
+        def result(self):
+            for f in futs:
+                f.result()
+            return arr
+
+    return _Result()
 
 
 def _filter(adata, cell_filter, gene_filter):
