@@ -2,9 +2,12 @@
 // (tc_stretch_begin / tc_cta_of in wotg_onthefly.cuh): for many grid shapes,
 // replays the kernel's walk over (row tile, column tile) pairs and the
 // combine's lookup, and checks that every (CTA, row tile) partial slot is
-// unique and inside the (CTAs + row tiles) x 128 buffer, and that the combine
-// of each row tile reads exactly the CTAs that wrote a partial for it.
-// Runs on the CPU; launches nothing.
+// unique and inside the (CTAs + row tiles) x 128 buffer, and that the merge
+// of each row tile reads exactly the CTAs that wrote a partial for it. The
+// in-kernel finish (CombineFin) counts 2 x (hi - lo + 1) partials per lane
+// quarter of a row tile (two column-half warps per covering CTA), so check 5
+// below is also the check of its expected count. Runs on the CPU; launches
+// nothing.
 #include <cstdio>
 #include <set>
 #include <vector>

@@ -24,8 +24,9 @@ def _run(name, tmp_path):
 
 
 def test_tensor_core_partition(tmp_path):
-    """lse_tc_kernel's stretches and the combine's partial lookup
-    (tc_stretch_begin / tc_cta_of): unique in-bounds slots, complete reads."""
+    """lse_tc_kernel's stretches and the merge's partial lookup
+    (tc_stretch_begin / tc_cta_of): unique in-bounds slots, complete reads,
+    and the number of writers per row tile that the in-kernel finish counts."""
     _run('stretch_check', tmp_path)
 
 
