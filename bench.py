@@ -227,7 +227,7 @@ def blas_threads():
 
 
 # The oracle's whole 20000 x 25000 solve, timed once on the GPU host's 16 cores with growth_iters = 1
-# (oracle/fullsize_c1.py; profiles/cpu_oracle_fullsize_20000x25000.md): too long for a bench step.
+# (oracle/fullsize_c1.py): too long for a bench step.
 CPU_FULL_SIZE = {'growth_iters': 1, 'iterations': 450, 'cost_s': 5.83, 'solve_s': 250.6, 'total_s': 256.4,
                  'cores': 16, 'per_iteration_vs_sample_extrapolation': 1.38}
 
@@ -257,7 +257,7 @@ def run_reference(args):
     # maps/s at full size from the sample's time scaled by I*J. The oracle's whole-pair solve, timed
     # once on the same host's 16 cores, spent 1.38x more time per Sinkhorn iteration than this
     # extrapolation assumes (its iterates no longer fit the caches): the value is an upper bound on
-    # the CPU's throughput (profiles/cpu_oracle_fullsize_20000x25000.md).
+    # the CPU's throughput (the whole-pair run is in the line as cpu_full_size_measured).
     value = 1.0 / (t_step * scale)
     sample = ('%dx%d random cell subsample of the 20000x25000 pair per step (own median), full FP64 oracle '
               'duality-gap solve x3 growth iterations (%.0f iterations); ms_per_step is the measured time of '
