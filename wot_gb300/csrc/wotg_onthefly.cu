@@ -175,25 +175,15 @@ int tc_ctas_per_sm(int kp) {
 int tc_parts() { return kTcParts; }
 
 int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int kp, int ctas, float2* part,
-                  const float* off, int* err, cudaStream_t st, uint32_t wait_tries, bool dependent) {
-  const float* no_w = nullptr;
-  float* no_s = nullptr;
+                  const float* off, int* err, cudaStream_t st, uint32_t wait_tries) {
   if (kp == 32) {
     WOTG_CUDA(tc_set_smem_attr<32>());
-    if (dependent)
-      WOTG_CUDA(launch_dependent(lse_tc_kernel<32, 0>, dim3(ctas), dim3(kTcThreads), TcSmem<32>::kAlloc, st, Pt, Qt,
-                                 n_ptiles, nq, part, off, err, wait_tries, no_w, 0, 0, no_s, NoFin{}));
-    else
-      lse_tc_kernel<32, 0><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
-                                                                          wait_tries, nullptr, 0, 0, nullptr, NoFin{});
+    lse_tc_kernel<32, 0><<<ctas, kTcThreads, TcSmem<32>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
+                                                                        wait_tries, nullptr, 0, 0, nullptr, NoFin{});
   } else if (kp == 64) {
     WOTG_CUDA(tc_set_smem_attr<64>());
-    if (dependent)
-      WOTG_CUDA(launch_dependent(lse_tc_kernel<64, 0>, dim3(ctas), dim3(kTcThreads), TcSmem<64>::kAlloc, st, Pt, Qt,
-                                 n_ptiles, nq, part, off, err, wait_tries, no_w, 0, 0, no_s, NoFin{}));
-    else
-      lse_tc_kernel<64, 0><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
-                                                                          wait_tries, nullptr, 0, 0, nullptr, NoFin{});
+    lse_tc_kernel<64, 0><<<ctas, kTcThreads, TcSmem<64>::kAlloc, st>>>(Pt, Qt, n_ptiles, nq, part, off, err,
+                                                                        wait_tries, nullptr, 0, 0, nullptr, NoFin{});
   } else {
     return WOTG_BADARG;
   }

@@ -82,9 +82,7 @@ int tc_parts();
 // wait_tries bounds each of the kernel's mbarrier waits (tries of up to 1 us);
 // a wait that runs out sets *err (see lse_tc_kernel).
 constexpr uint32_t kTcDefaultWaitTries = 4000000;
-// dependent: launched with programmatic stream serialisation (launch_dependent).
 int tc_lse_launch(const __half* Pt, int n_ptiles, const __half* Qt, int nq, int kp, int ctas, float2* part,
-                  const float* off, int* err, cudaStream_t st, uint32_t wait_tries = kTcDefaultWaitTries,
-                  bool dependent = false);
+                  const float* off, int* err, cudaStream_t st, uint32_t wait_tries = kTcDefaultWaitTries);
 
 }  // namespace wotg
