@@ -589,6 +589,29 @@ __global__ void stage_test_kernel(Geom g, Vecs V, Coef c, double* red) {
 //   acc[2] = sum_i (x log(x/p) - x + p)       acc[3] = sum_j (y log(y/q) - y + q)
 //   acc[4] = sum_i ubar x                      acc[5] = sum_j vbar y
 //   acc[6] = sum_i x
+// The gap terms of one point: x = exp(t) its marginal sum (t = log x), p its
+// target, the scaling a~ = exp(la) exp(u/eps) evaluated as the reference does.
+// Where nothing overflows or underflows, log(x / p) = t - log p and
+// log a~ = la + u/eps (to an ulp), which saves four of the six FP64
+// transcendentals per point (slow on this part); at the edges the reference's
+// own expressions run, so overflow, 0 log 0 and NaN behave as in the reference.
+__device__ __forceinline__ void gap_terms(double t, double la, double ue, double p, double logp, double lambda,
+                                          double eps, double* x_out, double* f_out, double* conj_out) {
+  const double x = exp(t);
+  double f, conj;
+  if (x > 0.0 && fabs(t) < 700.0 && fabs(la) < 700.0 && fabs(ue) < 700.0 && fabs(la + ue) < 700.0 && p > 0.0) {
+    f = x * (t - logp) - x + p;
+    conj = lambda * p * (exp(-eps * (la + ue) / lambda) - 1.0);
+  } else {
+    const double at = exp(la) * exp(ue);
+    f = x * log(x / p) - x + p;
+    conj = lambda * p * (exp(-eps * log(at) / lambda) - 1.0);
+  }
+  *x_out = x;
+  *f_out = f;
+  *conj_out = conj;
+}
+
 __global__ void gap_partial_kernel(Geom g, Vecs V, Coef c, double* red) {
   double acc[kNq];
 #pragma unroll
@@ -596,11 +619,10 @@ __global__ void gap_partial_kernel(Geom g, Vecs V, Coef c, double* red) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.I; i += stride) {
     const double ui = V.u[i], lai = V.la[i], pi = V.p[i];
-    const double x = exp(lai + ui * c.inv_eps + V.Lrow[i] - c.logJ);
+    const double ue = ui * c.inv_eps;
+    double x, f, conj;
+    gap_terms(lai + ue + V.Lrow[i] - c.logJ, lai, ue, pi, V.logp[i], c.lambda1, c.eps, &x, &f, &conj);
     const double ub = ui + c.eps * lai;
-    const double at = exp(lai) * exp(ui * c.inv_eps);
-    const double f = x * log(x / pi) - x + pi;
-    const double conj = c.lambda1 * pi * (exp(-c.eps * log(at) / c.lambda1) - 1.0);
     acc[0] += c.lambda1 * f + conj + ub * x;
     acc[2] += f;
     acc[4] += ub * x;
@@ -608,11 +630,10 @@ __global__ void gap_partial_kernel(Geom g, Vecs V, Coef c, double* red) {
   }
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.J; j += stride) {
     const double vj = V.v[j], lbj = V.lb[j];
-    const double y = exp(lbj + vj * c.inv_eps + V.Lcol[j] - c.logI);
+    const double ve = vj * c.inv_eps;
+    double y, f, conj;
+    gap_terms(lbj + ve + V.Lcol[j] - c.logI, lbj, ve, c.q, c.logq, c.lambda2, c.eps, &y, &f, &conj);
     const double vb = vj + c.eps * lbj;
-    const double bt = exp(lbj) * exp(vj * c.inv_eps);
-    const double f = y * log(y / c.q) - y + c.q;
-    const double conj = c.lambda2 * c.q * (exp(-c.eps * log(bt) / c.lambda2) - 1.0);
     acc[1] += c.lambda2 * f + conj + vb * y;
     acc[3] += f;
     acc[5] += vb * y;
