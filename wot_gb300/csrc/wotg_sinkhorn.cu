@@ -187,10 +187,21 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const float* __restrict__
     const float o = PREC ? grid_offset(V.Lrow[i]) : 0.f;
     float m = kNegBig, s = 0.f, cmp = 0.f;   // PREC: compensated sum s - cmp
     int64_t k = lane;
+    // the cost loads of the next 128-float4 chunk are issued before this
+    // chunk's arithmetic (two chunks of loads in flight per lane)
+    float4 cn[4];
+    if (k + 96 < nv) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) cn[t] = ld_stream(row + k + 32 * t);
+    }
     for (; k + 96 < nv; k += 128) {
       float4 cc[4], ww[4], wl[4];
 #pragma unroll
-      for (int t = 0; t < 4; ++t) cc[t] = ld_stream(row + k + 32 * t);
+      for (int t = 0; t < 4; ++t) cc[t] = cn[t];
+      if (k + 128 + 96 < nv) {
+#pragma unroll
+        for (int t = 0; t < 4; ++t) cn[t] = ld_stream(row + k + 128 + 32 * t);
+      }
 #pragma unroll
       for (int t = 0; t < 4; ++t) ww[t] = __ldg(w4 + k + 32 * t);
 #pragma unroll
@@ -287,11 +298,22 @@ __global__ void __launch_bounds__(256) col_partial_kernel(const float* __restric
   float s[4] = {0.f, 0.f, 0.f, 0.f};
   float cmp[4] = {0.f, 0.f, 0.f, 0.f};   // PREC: compensated sums s - cmp
   int64_t i = r0;
+  // the next chunk's cost loads are issued before this chunk's arithmetic
+  float4 cn[kColRowChunk];
+  if (i + kColRowChunk <= r1) {
+#pragma unroll
+    for (int t = 0; t < kColRowChunk; ++t) cn[t] = ld_stream(reinterpret_cast<const float4*>(C + (i + t) * g.ldc) + c4);
+  }
   for (; i + kColRowChunk <= r1; i += kColRowChunk) {
     float4 cc[kColRowChunk];
     float w[kColRowChunk], wl[kColRowChunk];
 #pragma unroll
-    for (int t = 0; t < kColRowChunk; ++t) cc[t] = ld_stream(reinterpret_cast<const float4*>(C + (i + t) * g.ldc) + c4);
+    for (int t = 0; t < kColRowChunk; ++t) cc[t] = cn[t];
+    if (i + 2 * kColRowChunk <= r1) {
+#pragma unroll
+      for (int t = 0; t < kColRowChunk; ++t)
+        cn[t] = ld_stream(reinterpret_cast<const float4*>(C + (i + kColRowChunk + t) * g.ldc) + c4);
+    }
 #pragma unroll
     for (int t = 0; t < kColRowChunk; ++t) w[t] = __ldg(V.wrow + i + t);
 #pragma unroll
