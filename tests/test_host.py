@@ -366,3 +366,28 @@ def test_objective_helpers_match_the_reference_forms():
     if not torch.cuda.is_available():
         with pytest.raises(RuntimeError, match='CUDA device'):
             wot_gb300.ot.primal(C, K, R, dx, dy, p, q, a, b, eps, l1, l2)
+
+
+def test_fma_pipe_exp2_coefficients_meet_their_bound_on_cpu():
+    """The FMA-pipe 2^z of the tensor-core epilogue (wotg_common.cuh::ex2_fma2),
+    replayed in NumPy FP32 with the coefficients read from the header: the
+    round-to-nearest reduction, the degree-5 Horner evaluation with one rounding
+    per fused multiply-add, and the exact power of two stay within 3e-7 of
+    2^z on [-125, 126] (the GPU test holds the kernel to the same bound)."""
+    import re
+    src = open(os.path.join(ROOT, 'wot_gb300', 'csrc', 'wotg_common.cuh')).read()
+    body = src[src.index('float2 ex2_fma2(float2 z)'):]
+    body = body[:body.index('return __fmul2_rn')]
+    coef = [float(v) for v in re.findall(r'make_float2\(([0-9.e+-]+)f, \1f\)', body)]
+    coef = [c for c in coef if abs(c) < 1e6]                 # drop the 1.5 * 2^23 shift constants
+    assert len(coef) == 6                                    # c5 first (Horner order) ... c0
+    z = np.concatenate([np.linspace(-125, 126, 1_000_003), np.linspace(-0.5, 0.5, 50_001)]).astype(np.float32)
+    t = (z + np.float32(12582912.0)).astype(np.float32)
+    n = (t - np.float32(12582912.0)).astype(np.float32)
+    f = (z - n).astype(np.float32)
+    p = np.float32(coef[0]) * np.ones_like(f)
+    for ck in coef[1:]:
+        p = (p.astype(np.float64) * f + np.float64(np.float32(ck))).astype(np.float32)   # one rounding per fma
+    r = (p.astype(np.float64) * np.exp2(n.astype(np.float64))).astype(np.float32)
+    ref = np.exp2(z.astype(np.float64))
+    assert np.abs(r.astype(np.float64) / ref - 1).max() <= 3e-7
